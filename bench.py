@@ -1,0 +1,420 @@
+#!/usr/bin/env python3
+"""Benchmark of the full BVH build (bounds -> Morton -> sort -> H-PLOC -> BVH8).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload clustered12m|sphere4m|soup65k] [--key-bits 30|63]
+                    [--radius 4|8|16]
+
+One step = one complete build of the workload.  The default workload is the
+plain clustered mesh: 12,582,912 triangles from 256 anisotropic Gaussians,
+63-bit Morton codes, H-PLOC radius 8 (the configuration the >=1.5x target is
+quoted on).  Inputs (453 MB) are larger than L2 (126 MB), so no flush is
+needed between steps.
+
+ours:      ``value`` = Mtris/s of nxb_build_async with the triangles resident
+           in HBM, timed with CUDA events on the launching stream over K
+           steps (per-stage events recorded on the same stream);
+           ``e2e`` = the same metric through the reference-shaped C-ABI call
+           nxb_build_bvh8 with the triangles in pinned host memory: each step
+           copies them to the device, builds (allocating outputs), reads the
+           result back and frees the BVH.
+reference: the reference's own CUDA build (NXB::BuildBVH8 compiled from its
+           sources into oracle/_ref/) on the same workload; its ``e2e`` adds
+           the host->device copy the same way.  If it is not built, the CPU
+           oracle port stands in (stated in the line).
+Multi-GPU: the build of one mesh does not shard; each rank builds its own
+replica (no collective) and ``value`` = total triangles / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    "clustered12m": ("clustered12m: 12,582,912 triangles, 256 anisotropic Gaussians, lognormal(-6,1) edges", 63),
+    "sphere4m": ("sphere4m: 4,194,304 triangles, 2048x1024 displaced UV sphere", 63),
+    "soup65k": ("soup65k: 65,536 triangles, uniform centroids, +-0.005 vertex offsets", 30),
+}
+
+# Algorithmic bytes per triangle of each stage (k = key bytes, P = passes):
+# bounds R36+W32; Morton R24 + W k + W4; sort 2P(k+4)+k; H-PLOC k+72;
+# BVH8 84 + 80 * (BVH8 nodes / n).
+STAGES = ["scene_bounds", "morton", "radix_sort", "hploc", "bvh8"]
+
+
+def algorithmic_bytes(stage: str, k: int, passes: int, bvh8_nodes_per_tri: float) -> float:
+    return {
+        "scene_bounds": 68.0,
+        "morton": 28.0 + k,
+        "radix_sort": 2.0 * passes * (k + 4) + k,
+        "hploc": k + 72.0,
+        "bvh8": 84.0 + 80.0 * bvh8_nodes_per_tri,
+    }[stage]
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc:
+            time.sleep(0.3)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (getattr(self, "out", "") or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        loaded = [s for s in sm if s > 0.5 * mx] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_prims(name: str) -> np.ndarray:
+    from nexusbvh_gb300 import scenes
+    return scenes.by_name(name)
+
+
+def cpu_baseline(prims: np.ndarray, key_bits: int, radius: int, sample: int) -> dict:
+    """The CPU oracle (multithreaded restatement) on a bounded prefix sample."""
+    import oracle
+    m = min(sample, prims.shape[0])
+    sub = np.ascontiguousarray(prims[:m])
+    t = time.perf_counter()
+    r = oracle.build(sub, key_bits, radius)
+    dt = time.perf_counter() - t
+    assert r["err"] == 0
+    return {"value": round(m / dt / 1e6, 3), "unit": "Mtris/s", "cores": oracle.threads(), "kind": "port",
+            "sample": f"first {m:,} triangles of the workload, one full CPU build (bounds, Morton, radix sort, "
+                      f"H-PLOC, BVH8) in {dt:.2f} s",
+            "stage_ms": [round(x, 1) for x in r["stage_ms"]]}
+
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    import nexusbvh_gb300 as nxb
+
+    torch.cuda.set_device(local)
+    lib = nxb.load()
+    prims_np = make_prims(args.workload)
+    n = prims_np.shape[0]
+    key_bits = args.key_bits
+    kb = 4 if key_bits == 30 else 8
+    passes = 4 if key_bits == 30 else 8
+    cfg = nxb.BuildConfig(prioritize_speed=key_bits == 30, search_radius=args.radius)
+    c = cfg.to_c()
+    d_prims = torch.from_numpy(prims_np).cuda()
+    b = nxb.Builder()
+    sz = b.sizes(n, cfg)
+    ws = b.workspace(sz.workspace_bytes)
+    b2 = torch.empty((sz.bvh2_node_count, 32), dtype=torch.uint8, device="cuda")
+    b8 = torch.empty((sz.bvh8_node_capacity, 80), dtype=torch.uint8, device="cuda")
+    prim_idx = torch.empty(n, dtype=torch.int32, device="cuda")
+    res = torch.zeros(64, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    sptr = int(stream.cuda_stream)
+
+    def enqueue(events=None):
+        args_ = (d_prims.data_ptr(), nxb.NXB_PRIM_TRIANGLE, n, ctypes.byref(c), ws.data_ptr(), ws.numel(),
+                 b2.data_ptr(), b8.data_ptr(), prim_idx.data_ptr(), res.data_ptr(), sptr)
+        if events is None:
+            nxb.check(lib.nxb_build_async(*args_), "nxb_build_async")
+        else:
+            nxb.check(lib.nxb_build_async_timed(*args_, events), "nxb_build_async_timed")
+
+    for _ in range(args.warmup):
+        enqueue()
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(args.steps)]
+    ev_arrays = [(ctypes.c_void_p * 6)(*[e.cuda_event for e in row]) for row in evs]
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        start.record(stream)
+        for k in range(args.steps):
+            enqueue(ev_arrays[k])
+        stop.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    elapsed = start.elapsed_time(stop)
+    if world > 1:
+        t = torch.tensor([elapsed], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed = float(t.item())
+    result = nxb.CResult.from_buffer_copy(res.cpu().numpy().tobytes())
+    if result.error_word:
+        raise RuntimeError(f"device error word {result.error_word:#x}")
+    stage_ms = {s: statistics.mean(evs[k][i].elapsed_time(evs[k][i + 1]) for k in range(args.steps))
+                for i, s in enumerate(STAGES)}
+    ms_per_step = elapsed / args.steps
+    value = world * n * args.steps / elapsed / 1e3  # Mtris/s
+
+    # e2e: host data, reference-shaped C-ABI call, result read back
+    h_prims = torch.from_numpy(prims_np).pin_memory()
+    d_in = torch.empty_like(d_prims)
+    out = nxb.CBVH8()
+    for _ in range(2):
+        d_in.copy_(h_prims, non_blocking=True)
+        nxb.check(lib.nxb_build_bvh8(d_in.data_ptr(), nxb.NXB_PRIM_TRIANGLE, n, ctypes.byref(c), sptr,
+                                     ctypes.byref(out), None), "nxb_build_bvh8")
+        nxb.check(lib.nxb_free_device_bvh8(ctypes.byref(out)), "nxb_free_device_bvh8")
+    e2e_steps = max(3, min(args.steps, 10))
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        d_in.copy_(h_prims, non_blocking=True)
+        nxb.check(lib.nxb_build_bvh8(d_in.data_ptr(), nxb.NXB_PRIM_TRIANGLE, n, ctypes.byref(c), sptr,
+                                     ctypes.byref(out), None), "nxb_build_bvh8")
+        nxb.check(lib.nxb_free_device_bvh8(ctypes.byref(out)), "nxb_free_device_bvh8")
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * n * e2e_steps / e2e_s / 1e6
+
+    if rank != 0:
+        return
+    pk = peaks()
+    n8_per_tri = result.bvh8_node_count / n
+    per_stage = {}
+    for s in STAGES:
+        byts = algorithmic_bytes(s, kb, passes, n8_per_tri) * n
+        gbs = byts / (stage_ms[s] * 1e-3) / 1e9
+        per_stage[s] = {"ms": round(stage_ms[s], 4), "alg_bytes": int(byts), "gbs": round(gbs, 1),
+                        "frac": round(gbs / pk["hbm_gbs"], 3)}
+    dominant = max(STAGES, key=lambda s: stage_ms[s])
+    traffic = None
+    tp = ROOT / "profiles" / "dram_traffic.json"
+    if tp.exists():
+        tj = json.loads(tp.read_text())
+        key = f"{args.workload}/{key_bits}/{dominant}"
+        if key in tj:
+            traffic = int(tj[key]["bytes_per_tri"] * n)
+    line = {
+        "metric": "Mtris/s full build (bounds, Morton, radix sort, H-PLOC BVH2, BVH8)",
+        "value": round(value, 2),
+        "unit": "Mtris/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_per_step, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded generators standing in for the reference's scene files)",
+        "config": {
+            "workload": WORKLOADS[args.workload][0],
+            "n_tris": n,
+            "key_bits": key_bits,
+            "search_radius": args.radius,
+            "parallelism": f"replicas x{world} (one mesh per GPU, no collective)",
+            "l2": "inputs larger than L2 (triangles 36 B x n, no flush needed)",
+            "stage_ms": {s: per_stage[s]["ms"] for s in STAGES},
+            "stage_sum_ms": round(sum(stage_ms.values()), 4),
+            "stage_roofline": per_stage,
+            "bvh8_nodes": int(result.bvh8_node_count),
+        },
+        "roofline": {
+            "kernel": dominant,
+            "bound": "hbm",
+            "achieved": per_stage[dominant]["gbs"],
+            "peak": pk["hbm_gbs"],
+            "unit": "GB/s",
+            "frac": per_stage[dominant]["frac"],
+            "traffic": traffic,
+            "peak_source": pk["source"],
+        },
+        "e2e": {"value": round(e2e_value, 2), "unit": "Mtris/s", "h2d_bytes_per_step": 36 * n,
+                "d2h_bytes_per_step": ctypes.sizeof(nxb.CResult),
+                "call": "nxb_build_bvh8 (C ABI, allocates outputs) after a pinned host->device copy"},
+        "gpu_launches": (6 + passes) * args.steps,
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(prims_np, key_bits, args.radius, args.cpu_sample)
+    print(json.dumps(line), flush=True)
+
+
+def run_reference(args, world, rank, local):
+    if rank != 0:
+        return
+    import torch
+
+    torch.cuda.set_device(local)
+    prims_np = make_prims(args.workload)
+    n = prims_np.shape[0]
+    key_bits = args.key_bits
+    line = {"metric": "Mtris/s full build (bounds, Morton, radix sort, H-PLOC BVH2, BVH8)", "unit": "Mtris/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "impl": "reference",
+            "data": "synthetic (seeded generators standing in for the reference's scene files)",
+            "config": {"workload": WORKLOADS[args.workload][0], "n_tris": n, "key_bits": key_bits,
+                       "search_radius": args.radius,
+                       "l2": "inputs larger than L2 (triangles 36 B x n, no flush needed)"}}
+    from oracle import build_ref
+    libp = build_ref.lib_path(args.radius)
+    if not libp.exists():
+        try:
+            build_ref.build()
+        except Exception:
+            pass
+    if not libp.exists():
+        # the reference's own build is unavailable: time the CPU port instead
+        cb = cpu_baseline(prims_np, key_bits, args.radius, args.cpu_sample)
+        line.update(value=cb["value"], ms_per_step=None, cpu_baseline=cb,
+                    e2e={"value": cb["value"], "unit": "Mtris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                    note="reference CUDA build not available here; the CPU oracle port was timed")
+        print(json.dumps(line), flush=True)
+        return
+    lib = ctypes.CDLL(str(libp))
+    P, U = ctypes.c_void_p, ctypes.c_uint32
+    lib.ref_build_bvh8.argtypes = [P, ctypes.c_int, U, ctypes.c_int, P, P, P, P, P]
+    lib.ref_e2e_bvh8.argtypes = [P, ctypes.c_size_t, P, ctypes.c_int, U, ctypes.c_int, P]
+    ps = 1 if key_bits == 30 else 0
+    d_prims = torch.from_numpy(prims_np).cuda()
+    nc = U(0)
+    for _ in range(args.warmup):
+        assert lib.ref_build_bvh8(d_prims.data_ptr(), 1, n, ps, None, None, ctypes.byref(nc), None, None) == 0
+    # the reference's own definition: sum of its per-stage event times
+    m9 = (ctypes.c_float * 9)()
+    stage = []
+    for _ in range(3):
+        assert lib.ref_build_bvh8(d_prims.data_ptr(), 1, n, ps, None, None, ctypes.byref(nc), None, m9) == 0
+        stage.append(list(m9))
+    stage = np.mean(np.array(stage), axis=0)
+    torch.cuda.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        start.record()
+        for _ in range(args.steps):
+            assert lib.ref_build_bvh8(d_prims.data_ptr(), 1, n, ps, None, None, ctypes.byref(nc), None, None) == 0
+        stop.record()
+        torch.cuda.synchronize()
+    elapsed = start.elapsed_time(stop)
+    h = torch.from_numpy(prims_np).pin_memory()
+    e2e_steps = max(3, min(args.steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        assert lib.ref_e2e_bvh8(h.data_ptr(), 36 * n, d_prims.data_ptr(), 1, n, ps, ctypes.byref(nc)) == 0
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    value = n * args.steps / elapsed / 1e3
+    line.update(
+        value=round(value, 2), ms_per_step=round(elapsed / args.steps, 4),
+        e2e={"value": round(n * e2e_steps / e2e_s / 1e6, 2), "unit": "Mtris/s", "h2d_bytes_per_step": 36 * n,
+             "d2h_bytes_per_step": 4, "call": "NXB::BuildBVH8<Triangle> after a pinned host->device copy"},
+        cpu_baseline={"value": round(value, 2), "unit": "Mtris/s", "cores": 0, "kind": "reference",
+                      "sample": "full workload; the reference path is CUDA code on the GPU (host cores only "
+                                "orchestrate); built from its sources with its own flags"},
+        reference_stage_ms={"scene_bounds": float(stage[0]), "morton": float(stage[1]), "radix_sort": float(stage[2]),
+                            "hploc": float(stage[3]), "bvh8": float(stage[4]), "total": float(stage[5])},
+        reference_costs={"bvh2": float(stage[6]), "bvh8": float(stage[7])},
+        bvh8_nodes=int(nc.value), clocks=clocks.summary())
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="clustered12m")
+    ap.add_argument("--key-bits", type=int, choices=[30, 63], default=None)
+    ap.add_argument("--radius", type=int, choices=[4, 8, 16], default=8)
+    ap.add_argument("--cpu-sample", type=int, default=2_000_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.key_bits is None:
+        args.key_bits = WORKLOADS[args.workload][1]
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist()
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
+    try:
+        if args.impl == "reference":
+            run_reference(args, world, rank, local)
+        else:
+            run_ours(args, world, rank, local)
+    finally:
+        if world > 1:
+            import torch
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

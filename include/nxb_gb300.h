@@ -1,0 +1,292 @@
+/*
+ * nxb_gb300.h - C ABI of the GB300 (sm_103a) BVH build pipeline.
+ *
+ * The pipeline is: scene bounds + leaf write -> 30/63-bit Morton codes ->
+ * stable key-value radix sort -> H-PLOC binary BVH (BVH2) -> compressed
+ * 8-wide BVH (BVH8, 80-byte nodes with 8-bit quantised child boxes).
+ *
+ * Every entry point takes plain pointers and sizes, returns an nxb_status and
+ * never terminates the process.  Device pointers are CUDA global-memory
+ * pointers on the current device; every launch goes to the stream given
+ * (NULL = legacy default stream, which is what NexusBVH uses).
+ *
+ * Reference interfaces replaced (paths inside the NexusBVH project):
+ *   NXB::BuildBVH2<PrimT>   NexusBVH/include/NXB/BVHBuilder.h:18-31,
+ *                           NexusBVH/src/BVHBuilder.cpp:114-171
+ *   NXB::BuildBVH8<PrimT>   NexusBVH/include/NXB/BVHBuilder.h:32-43,
+ *                           NexusBVH/src/BVHBuilder.cpp:173-267
+ *   NXB::ToHost / FreeHostBVH / FreeDeviceBVH
+ *                           NexusBVH/include/NXB/BVHBuilder.h:45-55,
+ *                           NexusBVH/src/BVHBuilder.cpp:269-294
+ * The per-stage entry points (nxb_stage_*) replace the kernels the host
+ * builder launches one by one:
+ *   ComputeSceneBoundsKernel  NexusBVH/src/Cuda/Setup.cu:12-39
+ *   ComputeMortonCodesKernel  NexusBVH/src/Cuda/Setup.cu:42-59
+ *   RadixSort                 NexusBVH/src/Cuda/Setup.cu:62-112
+ *   BuildBVH2Kernel           NexusBVH/src/Cuda/BinaryBuilder.cu:200-273
+ *   BuildBVH8Kernel           NexusBVH/src/Cuda/WideConverter.cu:225-414
+ *   ComputeBVH2CostKernel / ComputeBVH8CostKernel
+ *                             NexusBVH/src/Cuda/Eval.cu:12-80
+ *
+ * The struct layouts below are byte-identical to the reference's
+ * NXB::AABB (24 B), NXB::Triangle (36 B), NXB::BVH2::Node (32 B),
+ * NXB::BVH8::Node (80 B), NXB::BVH2 (40 B), NXB::BVH8 (56 B) and
+ * NXB::BVHBuildMetrics (36 B) (NexusBVH/include/NXB/AABB.h:8-53,
+ * Triangle.h:10-47, BVH.h:8-96, BVHBuildMetrics.h:7-50), so arrays built
+ * here can be handed to code written against the reference unchanged.
+ */
+#ifndef NXB_GB300_H
+#define NXB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+struct CUstream_st; /* cudaStream_t is `struct CUstream_st*` */
+
+#define NXB_INVALID_IDX 0xFFFFFFFFu
+
+/* ------------------------------------------------------------------ status */
+typedef enum nxb_status {
+    NXB_OK = 0,
+    NXB_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad prim type, n == 0, ... */
+    NXB_ERR_UNSUPPORTED = 2,      /* a size or option this build does not support */
+    NXB_ERR_OUT_OF_MEMORY = 3,    /* a device allocation was refused */
+    NXB_ERR_CUDA = 4,             /* a CUDA runtime call failed (see nxb_last_cuda_error) */
+    NXB_ERR_WORKSPACE_TOO_SMALL = 5,
+    NXB_ERR_DEVICE_TIMEOUT = 6,   /* a bounded device-side wait gave up (error word set) */
+    NXB_ERR_DEVICE_INVARIANT = 7, /* a kernel found an impossible state (error word set) */
+    NXB_ERR_ADMISSION = 8         /* server: the request does not fit the memory budget */
+} nxb_status;
+
+/* Returns a static, human-readable name for a status code. */
+const char* nxb_status_string(nxb_status status);
+/* Last CUDA error code seen by this thread inside the library (0 if none). */
+int nxb_last_cuda_error(void);
+
+/* ------------------------------------------------------------------- types */
+/* Values match NXB::PrimType (NexusBVH/include/NXB/BVH.h:12-16). */
+typedef enum nxb_prim_type { NXB_PRIM_AABB = 0, NXB_PRIM_TRIANGLE = 1 } nxb_prim_type;
+
+typedef struct nxb_aabb {      /* NXB::AABB, 24 B */
+    float bmin[3];
+    float bmax[3];
+} nxb_aabb;
+
+typedef struct nxb_triangle {  /* NXB::Triangle, 36 B */
+    float v0[3], v1[3], v2[3];
+} nxb_triangle;
+
+typedef struct nxb_bvh2_node { /* NXB::BVH2::Node, 32 B */
+    nxb_aabb bounds;
+    uint32_t left;  /* NXB_INVALID_IDX for a leaf */
+    uint32_t right; /* primitive index for a leaf */
+} nxb_bvh2_node;
+
+typedef struct nxb_bvh8_node { /* NXB::BVH8::Node / NodeExplicit, 80 B */
+    float p[3];            /* origin of the child grid */
+    uint8_t e[3];          /* biased exponents of the grid scale */
+    uint8_t imask;         /* bit i: child slot i is an inner node */
+    uint32_t child_base;   /* index of the first inner child node */
+    uint32_t prim_base;    /* index of the first leaf in prim_idx[] */
+    uint8_t meta[8];       /* 0 = empty; 0x20|(24+i) inner; 0x20|rank leaf */
+    uint8_t qlo[3][8];     /* qlox, qloy, qloz */
+    uint8_t qhi[3][8];     /* qhix, qhiy, qhiz */
+} nxb_bvh8_node;
+
+typedef struct nxb_bvh2 {      /* NXB::BVH2, 40 B */
+    nxb_bvh2_node* nodes;  /* 2n-1 nodes: leaves [0,n), internal [n,2n-1), root 2n-2 */
+    uint32_t node_count;
+    uint32_t prim_count;
+    nxb_aabb bounds;       /* root (= scene) bounds, host copy */
+} nxb_bvh2;
+
+typedef struct nxb_bvh8 {      /* NXB::BVH8, 56 B */
+    nxb_bvh8_node* nodes;  /* root is node 0 */
+    uint32_t node_count;
+    uint32_t* prim_idx;    /* n entries, one primitive per leaf */
+    uint32_t prim_count;
+    nxb_aabb bounds;
+} nxb_bvh8;
+
+/* NXB::BVHBuildMetrics (NexusBVH/include/NXB/BVHBuildMetrics.h:7-50), 36 B.
+ * Times are CUDA-event milliseconds per stage; total_time is the sum of the
+ * stage times, exactly as the reference defines it
+ * (NexusBVH/src/BVHBuilder.cpp:75-76,223). Costs are only filled when
+ * metrics are requested. */
+typedef struct nxb_build_metrics {
+    float scene_bounds_time;
+    float morton_codes_time;
+    float radix_sort_time;
+    float bvh2_build_time;
+    float bvh8_conversion_time;
+    float total_time;
+    float bvh2_cost;
+    float bvh8_cost;
+    float average_child_per_node;
+} nxb_build_metrics;
+
+/* NXB::BuildConfig (NexusBVH/include/NXB/BuildConfig.h:6-12) plus the knobs
+ * the reference fixes at compile time (SEARCH_RADIUS, BinaryBuilder.cu:9).
+ * Zero-initialise and set what you need: zero means "reference default". */
+typedef struct nxb_build_config {
+    uint32_t prioritize_speed; /* nonzero: 30-bit Morton in 32-bit keys; else 63-bit in 64-bit keys */
+    uint32_t search_radius;    /* H-PLOC nearest-neighbour radius: 0 (= 8), 4, 8 or 16 */
+    uint32_t flags;            /* reserved, must be 0 */
+    uint32_t reserved;
+} nxb_build_config;
+
+/* -------------------------------------------- reference-shaped entry points */
+/* Builds a BVH2 from n device primitives (nxb_triangle or nxb_aabb).  The
+ * input is not modified.  out->nodes is allocated here (stream-ordered) and
+ * owned by the caller (nxb_free_device_bvh2).  Synchronises the stream before
+ * returning, like the reference.  metrics may be NULL; when given, stage
+ * times are measured with CUDA events and the SAH cost is computed. */
+nxb_status nxb_build_bvh2(const void* d_prims, nxb_prim_type prim_type, uint32_t prim_count,
+                          const nxb_build_config* config, struct CUstream_st* stream,
+                          nxb_bvh2* out_bvh, nxb_build_metrics* metrics);
+
+/* Builds a compressed BVH8 (through a BVH2 that is freed before returning).
+ * out->nodes and out->prim_idx are owned by the caller (nxb_free_device_bvh8). */
+nxb_status nxb_build_bvh8(const void* d_prims, nxb_prim_type prim_type, uint32_t prim_count,
+                          const nxb_build_config* config, struct CUstream_st* stream,
+                          nxb_bvh8* out_bvh, nxb_build_metrics* metrics);
+
+/* Synchronous device -> host copy of a BVH2 into malloc'd memory. */
+nxb_status nxb_bvh2_to_host(const nxb_bvh2* device_bvh, nxb_bvh2* host_bvh);
+nxb_status nxb_free_host_bvh2(nxb_bvh2* host_bvh);
+/* The same for a BVH8 (nodes and prim_idx).  The reference has no BVH8
+ * host export; this is the BVH2 ToHost contract applied to the BVH8. */
+nxb_status nxb_bvh8_to_host(const nxb_bvh8* device_bvh, nxb_bvh8* host_bvh);
+nxb_status nxb_free_host_bvh8(nxb_bvh8* host_bvh);
+nxb_status nxb_free_device_bvh2(nxb_bvh2* device_bvh);
+nxb_status nxb_free_device_bvh8(nxb_bvh8* device_bvh);
+
+/* ------------------------------------- allocation-free (workspace) builds */
+/* Sizes, in bytes, of what a build of prim_count primitives needs.  All
+ * device buffers must be 256-byte aligned (cudaMalloc alignment). */
+typedef struct nxb_build_sizes {
+    size_t workspace_bytes;  /* scratch: keys, values, sort state, counters */
+    size_t bvh2_node_count;  /* 2n-1 */
+    size_t bvh8_node_capacity; /* ceil((4n-1)/7), the reference's worst case */
+} nxb_build_sizes;
+
+nxb_status nxb_query_build_sizes(uint32_t prim_count, const nxb_build_config* config,
+                                 nxb_build_sizes* out_sizes);
+
+/* Device-side results of an asynchronous build (written by the kernels). */
+typedef struct nxb_build_result {
+    nxb_aabb scene_bounds;
+    uint32_t bvh8_node_count;
+    uint32_t bvh8_leaf_count;
+    uint32_t error_word;   /* 0 = fine; else an NXB_DEVERR_* bit set */
+    uint32_t bvh2_root;    /* 2n-2 */
+} nxb_build_result;
+
+#define NXB_DEVERR_SORT_LOOKBACK_TIMEOUT 0x1u
+#define NXB_DEVERR_BVH8_QUEUE_TIMEOUT    0x2u
+#define NXB_DEVERR_HPLOC_INVALID_CLUSTER 0x4u
+#define NXB_DEVERR_BVH8_OVERFLOW         0x8u
+
+/* Enqueues the whole BVH2 (+ optional BVH8) build on `stream` with no
+ * allocation, no host synchronisation and no host<->device copy, so it can
+ * be captured in a CUDA graph.  d_bvh8_nodes / d_prim_idx may be NULL to
+ * stop after the BVH2.  d_result receives the counters and the error word. */
+nxb_status nxb_build_async(const void* d_prims, nxb_prim_type prim_type, uint32_t prim_count,
+                           const nxb_build_config* config, void* d_workspace,
+                           size_t workspace_bytes, nxb_bvh2_node* d_bvh2_nodes,
+                           nxb_bvh8_node* d_bvh8_nodes, uint32_t* d_prim_idx,
+                           nxb_build_result* d_result, struct CUstream_st* stream);
+
+/* nxb_build_async that also records six caller-created CUDA events
+ * (cudaEvent_t handles) on `stream` at the stage boundaries: before scene
+ * bounds, after bounds, after Morton, after the sort, after H-PLOC, after
+ * the BVH8 collapse.  Used to time each stage on the launching stream. */
+nxb_status nxb_build_async_timed(const void* d_prims, nxb_prim_type prim_type, uint32_t prim_count,
+                                 const nxb_build_config* config, void* d_workspace,
+                                 size_t workspace_bytes, nxb_bvh2_node* d_bvh2_nodes,
+                                 nxb_bvh8_node* d_bvh8_nodes, uint32_t* d_prim_idx,
+                                 nxb_build_result* d_result, struct CUstream_st* stream,
+                                 void* const* stage_events);
+
+/* ------------------------------------------------------ per-stage entries */
+/* Stage 1 (ComputeSceneBoundsKernel): leaf i of d_nodes = {bounds(prim i),
+ * INVALID, i}; *d_scene = union of all leaf bounds. */
+nxb_status nxb_stage_scene_bounds(const void* d_prims, nxb_prim_type prim_type,
+                                  uint32_t prim_count, nxb_bvh2_node* d_nodes,
+                                  nxb_aabb* d_scene, struct CUstream_st* stream);
+
+/* Stage 2 (ComputeMortonCodesKernel): key i = Morton code of leaf i's
+ * centroid normalised by *d_scene (key_bits 30 -> uint32 keys, 63 -> uint64);
+ * d_cluster_idx[i] = i (may be NULL). */
+nxb_status nxb_stage_morton(const nxb_bvh2_node* d_nodes, uint32_t prim_count,
+                            const nxb_aabb* d_scene, uint32_t key_bits, void* d_keys,
+                            uint32_t* d_cluster_idx, struct CUstream_st* stream);
+
+/* Stage 3 (RadixSort): stable sort of (key, value) pairs by key bits
+ * [begin_bit, end_bit); full keys are carried.  Sorted output lands in
+ * d_keys_out / d_vals_out; the inputs are left unmodified.  d_vals_in NULL
+ * means values 0..n-1.  Scratch: nxb_sort_scratch_bytes(). */
+size_t nxb_sort_scratch_bytes(uint32_t count, uint32_t key_bytes, uint32_t begin_bit,
+                              uint32_t end_bit);
+nxb_status nxb_stage_radix_sort(uint32_t key_bytes, const void* d_keys_in, void* d_keys_out,
+                                const uint32_t* d_vals_in, uint32_t* d_vals_out,
+                                uint32_t count, uint32_t begin_bit, uint32_t end_bit,
+                                void* d_scratch, size_t scratch_bytes, uint32_t* d_error_word,
+                                struct CUstream_st* stream);
+
+/* Stage 4 (BuildBVH2Kernel): H-PLOC over sorted keys; d_cluster_idx is the
+ * sorted permutation (it is overwritten); d_nodes leaves [0,n) must hold the
+ * stage-1 output; internal nodes are written to [n, 2n-1).  Scratch:
+ * nxb_hploc_scratch_bytes(). */
+size_t nxb_hploc_scratch_bytes(uint32_t prim_count);
+nxb_status nxb_stage_hploc(uint32_t key_bytes, const void* d_sorted_keys,
+                           uint32_t* d_cluster_idx, nxb_bvh2_node* d_nodes,
+                           uint32_t prim_count, uint32_t search_radius, void* d_scratch,
+                           size_t scratch_bytes, uint32_t* d_error_word,
+                           struct CUstream_st* stream);
+
+/* Stage 5 (BuildBVH8Kernel): collapse the BVH2 rooted at node 2n-2 into a
+ * BVH8 rooted at node 0.  d_counts receives {node_count, leaf_count}.
+ * Scratch: nxb_bvh8_scratch_bytes(). */
+size_t nxb_bvh8_scratch_bytes(uint32_t prim_count);
+nxb_status nxb_stage_bvh8(const nxb_bvh2_node* d_bvh2_nodes, uint32_t prim_count,
+                          nxb_bvh8_node* d_bvh8_nodes, uint32_t* d_prim_idx,
+                          uint32_t* d_counts, void* d_scratch, size_t scratch_bytes,
+                          uint32_t* d_error_word, struct CUstream_st* stream);
+
+/* Cost evaluation (Eval.cu): SAH of a BVH2 (all 2n-1 nodes) and the cost of
+ * a BVH8 (children only), relative to the root area; *d_cost is overwritten. */
+nxb_status nxb_eval_bvh2_cost(const nxb_bvh2_node* d_nodes, uint32_t node_count,
+                              const nxb_aabb* d_root_bounds, float* d_cost,
+                              struct CUstream_st* stream);
+nxb_status nxb_eval_bvh8_cost(const nxb_bvh8_node* d_nodes, uint32_t node_count,
+                              const nxb_aabb* d_root_bounds, float* d_cost,
+                              struct CUstream_st* stream);
+
+/* Library version and the compile flags that define its numerics. */
+const char* nxb_version(void);
+
+/* Diagnostics: evaluates, on the current device, the plain source
+ * expressions whose rounding the reference's results depend on (box area
+ * FMA contraction, float -> uint8 quantisation, signed-zero min/max,
+ * fast-math division) next to the forms this library pins, and fills
+ * report[0..39] (layout in nexusbvh_gb300/csrc/eval.cu).  Allocates a few
+ * MB of device memory and synchronises the device. */
+nxb_status nxb_selftest_numerics(uint32_t* report, uint32_t report_len);
+
+/* Diagnostics: runs the two kernels that wait on other CTAs (the sort's
+ * look-back and the BVH8 work queue) on inputs where the awaited flag is
+ * never set, and returns in words[0..1] the error words their bounded
+ * waits set (NXB_DEVERR_SORT_LOOKBACK_TIMEOUT, NXB_DEVERR_BVH8_QUEUE_TIMEOUT).
+ * The context stays usable.  Takes about a second. */
+nxb_status nxb_selftest_bounded_waits(uint32_t* words);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* NXB_GB300_H */

@@ -1,0 +1,333 @@
+"""GB300 (sm_103a) BVH builder: Python host side over the C ABI.
+
+The build runs entirely in ``libnxb_gb300.so`` (hand-written CUDA kernels);
+this module only binds its C ABI (``include/nxb_gb300.h``) with ctypes and
+mirrors the reference's host interface (NexusBVH/include/NXB/BVHBuilder.h):
+
+    build_bvh2(prims, config, metrics)  ~ NXB::BuildBVH2<PrimT>
+    build_bvh8(prims, config, metrics)  ~ NXB::BuildBVH8<PrimT>
+
+``prims`` is a CUDA tensor of float32 triangles ``[n, 9]`` (``NXB::Triangle``)
+or boxes ``[n, 6]`` (``NXB::AABB``).  The returned BVHs hold CUDA tensors
+whose bytes are the reference's node layouts.  There is no CPU path: if the
+library is missing, importing the functions raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+from pathlib import Path
+
+import numpy as np
+
+_LIB_PATH = Path(__file__).resolve().parent / "libnxb_gb300.so"
+_lib = None
+
+NXB_OK = 0
+NXB_PRIM_AABB = 0
+NXB_PRIM_TRIANGLE = 1
+INVALID_IDX = 0xFFFFFFFF
+
+STATUS_NAMES = {
+    0: "NXB_OK", 1: "NXB_ERR_INVALID_ARGUMENT", 2: "NXB_ERR_UNSUPPORTED", 3: "NXB_ERR_OUT_OF_MEMORY",
+    4: "NXB_ERR_CUDA", 5: "NXB_ERR_WORKSPACE_TOO_SMALL", 6: "NXB_ERR_DEVICE_TIMEOUT",
+    7: "NXB_ERR_DEVICE_INVARIANT", 8: "NXB_ERR_ADMISSION",
+}
+
+# numpy views of the device layouts
+BVH2_NODE_DTYPE = np.dtype([("bmin", "<f4", 3), ("bmax", "<f4", 3), ("left", "<u4"), ("right", "<u4")])
+BVH8_NODE_DTYPE = np.dtype([("p", "<f4", 3), ("e", "u1", 3), ("imask", "u1"), ("child_base", "<u4"),
+                            ("prim_base", "<u4"), ("meta", "u1", 8), ("qlo", "u1", (3, 8)), ("qhi", "u1", (3, 8))])
+assert BVH2_NODE_DTYPE.itemsize == 32 and BVH8_NODE_DTYPE.itemsize == 80
+
+
+class NxbError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        super().__init__(f"{what}: {STATUS_NAMES.get(status, status)}")
+
+
+class CAABB(ctypes.Structure):
+    _fields_ = [("bmin", ctypes.c_float * 3), ("bmax", ctypes.c_float * 3)]
+
+
+class CBVH2(ctypes.Structure):
+    _fields_ = [("nodes", ctypes.c_void_p), ("node_count", ctypes.c_uint32), ("prim_count", ctypes.c_uint32),
+                ("bounds", CAABB)]
+
+
+class CBVH8(ctypes.Structure):
+    _fields_ = [("nodes", ctypes.c_void_p), ("node_count", ctypes.c_uint32), ("prim_idx", ctypes.c_void_p),
+                ("prim_count", ctypes.c_uint32), ("bounds", CAABB)]
+
+
+class CMetrics(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_float) for name in (
+        "scene_bounds_time", "morton_codes_time", "radix_sort_time", "bvh2_build_time", "bvh8_conversion_time",
+        "total_time", "bvh2_cost", "bvh8_cost", "average_child_per_node")]
+
+
+class CConfig(ctypes.Structure):
+    _fields_ = [("prioritize_speed", ctypes.c_uint32), ("search_radius", ctypes.c_uint32),
+                ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class CSizes(ctypes.Structure):
+    _fields_ = [("workspace_bytes", ctypes.c_size_t), ("bvh2_node_count", ctypes.c_size_t),
+                ("bvh8_node_capacity", ctypes.c_size_t)]
+
+
+class CResult(ctypes.Structure):
+    _fields_ = [("scene_bounds", CAABB), ("bvh8_node_count", ctypes.c_uint32), ("bvh8_leaf_count", ctypes.c_uint32),
+                ("error_word", ctypes.c_uint32), ("bvh2_root", ctypes.c_uint32)]
+
+
+assert ctypes.sizeof(CBVH2) == 40 and ctypes.sizeof(CBVH8) == 56 and ctypes.sizeof(CMetrics) == 36
+
+_P = ctypes.c_void_p
+_U32 = ctypes.c_uint32
+_SIG = {
+    "nxb_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "nxb_last_cuda_error": (ctypes.c_int, []),
+    "nxb_version": (ctypes.c_char_p, []),
+    "nxb_build_bvh2": (ctypes.c_int, [_P, ctypes.c_int, _U32, _P, _P, ctypes.POINTER(CBVH2), _P]),
+    "nxb_build_bvh8": (ctypes.c_int, [_P, ctypes.c_int, _U32, _P, _P, ctypes.POINTER(CBVH8), _P]),
+    "nxb_bvh2_to_host": (ctypes.c_int, [ctypes.POINTER(CBVH2), ctypes.POINTER(CBVH2)]),
+    "nxb_bvh8_to_host": (ctypes.c_int, [ctypes.POINTER(CBVH8), ctypes.POINTER(CBVH8)]),
+    "nxb_free_host_bvh2": (ctypes.c_int, [ctypes.POINTER(CBVH2)]),
+    "nxb_free_host_bvh8": (ctypes.c_int, [ctypes.POINTER(CBVH8)]),
+    "nxb_free_device_bvh2": (ctypes.c_int, [ctypes.POINTER(CBVH2)]),
+    "nxb_free_device_bvh8": (ctypes.c_int, [ctypes.POINTER(CBVH8)]),
+    "nxb_query_build_sizes": (ctypes.c_int, [_U32, _P, ctypes.POINTER(CSizes)]),
+    "nxb_build_async": (ctypes.c_int, [_P, ctypes.c_int, _U32, _P, _P, ctypes.c_size_t, _P, _P, _P, _P, _P]),
+    "nxb_build_async_timed": (ctypes.c_int, [_P, ctypes.c_int, _U32, _P, _P, ctypes.c_size_t, _P, _P, _P, _P, _P,
+                                             _P]),
+    "nxb_stage_scene_bounds": (ctypes.c_int, [_P, ctypes.c_int, _U32, _P, _P, _P]),
+    "nxb_stage_morton": (ctypes.c_int, [_P, _U32, _P, _U32, _P, _P, _P]),
+    "nxb_sort_scratch_bytes": (ctypes.c_size_t, [_U32, _U32, _U32, _U32]),
+    "nxb_stage_radix_sort": (ctypes.c_int, [_U32, _P, _P, _P, _P, _U32, _U32, _U32, _P, ctypes.c_size_t, _P, _P]),
+    "nxb_hploc_scratch_bytes": (ctypes.c_size_t, [_U32]),
+    "nxb_stage_hploc": (ctypes.c_int, [_U32, _P, _P, _P, _U32, _U32, _P, ctypes.c_size_t, _P, _P]),
+    "nxb_bvh8_scratch_bytes": (ctypes.c_size_t, [_U32]),
+    "nxb_stage_bvh8": (ctypes.c_int, [_P, _U32, _P, _P, _P, _P, ctypes.c_size_t, _P, _P]),
+    "nxb_eval_bvh2_cost": (ctypes.c_int, [_P, _U32, _P, _P, _P]),
+    "nxb_eval_bvh8_cost": (ctypes.c_int, [_P, _U32, _P, _P, _P]),
+    "nxb_selftest_numerics": (ctypes.c_int, [_P, _U32]),
+    "nxb_selftest_bounded_waits": (ctypes.c_int, [_P]),
+}
+
+
+def lib_path() -> Path:
+    return _LIB_PATH
+
+
+def load() -> ctypes.CDLL:
+    """Loads libnxb_gb300.so (built by ``__graft_entry__.build()``); raises if absent."""
+    global _lib
+    if _lib is None:
+        if not _LIB_PATH.exists():
+            raise RuntimeError(f"{_LIB_PATH.name} is not built: run __graft_entry__.build() (there is no CPU path)")
+        lib = ctypes.CDLL(str(_LIB_PATH))
+        for name, (res, args) in _SIG.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def check(status: int, what: str) -> None:
+    if status != NXB_OK:
+        raise NxbError(status, what)
+
+
+def _stream_ptr(stream=None) -> int:
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return int(s.cuda_stream)
+
+
+@dataclasses.dataclass
+class BuildConfig:
+    """NXB::BuildConfig plus the H-PLOC search radius (compile-time in the reference)."""
+    prioritize_speed: bool = False
+    search_radius: int = 8
+
+    def to_c(self) -> CConfig:
+        return CConfig(1 if self.prioritize_speed else 0, int(self.search_radius), 0, 0)
+
+    @property
+    def key_bits(self) -> int:
+        return 30 if self.prioritize_speed else 63
+
+
+@dataclasses.dataclass
+class BVHBuildMetrics:
+    """NXB::BVHBuildMetrics: per-stage CUDA-event milliseconds and costs."""
+    scene_bounds_time: float = 0.0
+    morton_codes_time: float = 0.0
+    radix_sort_time: float = 0.0
+    bvh2_build_time: float = 0.0
+    bvh8_conversion_time: float = 0.0
+    total_time: float = 0.0
+    bvh2_cost: float = 0.0
+    bvh8_cost: float = 0.0
+    average_child_per_node: float = 0.0
+
+    @classmethod
+    def from_c(cls, m: CMetrics) -> "BVHBuildMetrics":
+        return cls(**{f.name: float(getattr(m, f.name)) for f in dataclasses.fields(cls)})
+
+
+def prim_type_of(prims) -> int:
+    if prims.dim() != 2 or prims.shape[1] not in (6, 9):
+        raise ValueError("prims must be [n, 9] float32 triangles or [n, 6] float32 boxes")
+    return NXB_PRIM_TRIANGLE if prims.shape[1] == 9 else NXB_PRIM_AABB
+
+
+@dataclasses.dataclass
+class BVH2:
+    nodes: object          # torch uint8 CUDA tensor [2n-1, 32]
+    node_count: int
+    prim_count: int
+    bounds: tuple          # (bmin, bmax)
+
+    @property
+    def root(self) -> int:
+        return self.node_count - 1
+
+
+@dataclasses.dataclass
+class BVH8:
+    nodes: object          # torch uint8 CUDA tensor [node_count, 80]
+    node_count: int
+    prim_idx: object       # torch int32 CUDA tensor [n]
+    prim_count: int
+    bounds: tuple
+    bvh2: BVH2 | None = None
+
+
+class Builder:
+    """Keeps a workspace resident across builds and drives ``nxb_build_async``.
+
+    The build enqueues on the current torch stream with no allocation inside
+    the library; results are torch CUDA tensors.
+    """
+
+    def __init__(self):
+        load()
+        self._ws = None
+
+    def sizes(self, n: int, config: BuildConfig) -> CSizes:
+        s = CSizes()
+        c = config.to_c()
+        check(load().nxb_query_build_sizes(n, ctypes.byref(c), ctypes.byref(s)), "nxb_query_build_sizes")
+        return s
+
+    def workspace(self, nbytes: int):
+        import torch
+        if self._ws is None or self._ws.numel() < nbytes:
+            self._ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+        return self._ws
+
+    def enqueue(self, prims, n, config, ws, bvh2_nodes, bvh8_nodes, prim_idx, result, stream=None) -> None:
+        c = config.to_c()
+        check(load().nxb_build_async(
+            prims.data_ptr(), prim_type_of(prims), n, ctypes.byref(c), ws.data_ptr(), ws.numel(),
+            bvh2_nodes.data_ptr(), bvh8_nodes.data_ptr() if bvh8_nodes is not None else None,
+            prim_idx.data_ptr() if prim_idx is not None else None, result.data_ptr(), _stream_ptr(stream)),
+            "nxb_build_async")
+
+    def build(self, prims, config: BuildConfig = BuildConfig(), wide: bool = True):
+        import torch
+        n = int(prims.shape[0])
+        s = self.sizes(n, config)
+        ws = self.workspace(s.workspace_bytes)
+        bvh2_nodes = torch.empty((s.bvh2_node_count, 32), dtype=torch.uint8, device="cuda")
+        bvh8_nodes = torch.empty((s.bvh8_node_capacity, 80), dtype=torch.uint8, device="cuda") if wide else None
+        prim_idx = torch.empty(n, dtype=torch.int32, device="cuda") if wide else None
+        result = torch.zeros(ctypes.sizeof(CResult), dtype=torch.uint8, device="cuda")
+        self.enqueue(prims, n, config, ws, bvh2_nodes, bvh8_nodes, prim_idx, result)
+        r = CResult.from_buffer_copy(result.cpu().numpy().tobytes())
+        if r.error_word:
+            raise NxbError(7 if not (r.error_word & 3) else 6, f"device error word 0x{r.error_word:x}")
+        bounds = (tuple(r.scene_bounds.bmin), tuple(r.scene_bounds.bmax))
+        b2 = BVH2(bvh2_nodes, int(s.bvh2_node_count), n, bounds)
+        if not wide:
+            return b2
+        return BVH8(bvh8_nodes[: r.bvh8_node_count], int(r.bvh8_node_count), prim_idx, n, bounds, b2)
+
+
+def build_bvh2(prims, config: BuildConfig = BuildConfig(), metrics: BVHBuildMetrics | None = None) -> BVH2:
+    """NXB::BuildBVH2 through ``nxb_build_bvh2`` (library-owned output, copied into a torch tensor)."""
+    out = _build_plain(prims, config, metrics, wide=False)
+    return out
+
+
+def build_bvh8(prims, config: BuildConfig = BuildConfig(), metrics: BVHBuildMetrics | None = None) -> BVH8:
+    """NXB::BuildBVH8 through ``nxb_build_bvh8`` (library-owned output, copied into torch tensors)."""
+    return _build_plain(prims, config, metrics, wide=True)
+
+
+def _build_plain(prims, config, metrics, wide):
+    import torch
+    lib = load()
+    n = int(prims.shape[0])
+    c = config.to_c()
+    m = CMetrics()
+    mp = ctypes.byref(m) if metrics is not None else None
+    stream = _stream_ptr()
+    if wide:
+        out = CBVH8()
+        check(lib.nxb_build_bvh8(prims.data_ptr(), prim_type_of(prims), n, ctypes.byref(c), stream,
+                                 ctypes.byref(out), mp), "nxb_build_bvh8")
+        nodes = torch.empty((out.node_count, 80), dtype=torch.uint8, device="cuda")
+        prim_idx = torch.empty(n, dtype=torch.int32, device="cuda")
+        _copy_d2d(nodes.data_ptr(), out.nodes, out.node_count * 80)
+        _copy_d2d(prim_idx.data_ptr(), out.prim_idx, n * 4)
+        bounds = (tuple(out.bounds.bmin), tuple(out.bounds.bmax))
+        check(lib.nxb_free_device_bvh8(ctypes.byref(out)), "nxb_free_device_bvh8")
+        res = BVH8(nodes, int(out.node_count), prim_idx, n, bounds)
+    else:
+        out = CBVH2()
+        check(lib.nxb_build_bvh2(prims.data_ptr(), prim_type_of(prims), n, ctypes.byref(c), stream,
+                                 ctypes.byref(out), mp), "nxb_build_bvh2")
+        nodes = torch.empty((out.node_count, 32), dtype=torch.uint8, device="cuda")
+        _copy_d2d(nodes.data_ptr(), out.nodes, out.node_count * 32)
+        bounds = (tuple(out.bounds.bmin), tuple(out.bounds.bmax))
+        check(lib.nxb_free_device_bvh2(ctypes.byref(out)), "nxb_free_device_bvh2")
+        res = BVH2(nodes, int(out.node_count), n, bounds)
+    if metrics is not None:
+        for f in dataclasses.fields(BVHBuildMetrics):
+            setattr(metrics, f.name, float(getattr(m, f.name)))
+    return res
+
+
+def _copy_d2d(dst: int, src: int, nbytes: int) -> None:
+    import torch
+    if nbytes == 0:
+        return
+    # wrap the library-owned pointer without taking ownership
+    src_t = _borrow(src, nbytes)
+    dst_t = _borrow(dst, nbytes)
+    dst_t.copy_(src_t)
+    torch.cuda.synchronize()
+
+
+def _borrow(ptr: int, nbytes: int):
+    import torch
+    cls = type("_CudaArray", (), {})
+    obj = cls()
+    obj.__cuda_array_interface__ = {"shape": (nbytes,), "typestr": "|u1", "data": (ptr, False), "version": 3,
+                                    "strides": None}
+    return torch.as_tensor(obj, device="cuda")
+
+
+def selftest_numerics() -> list[int]:
+    rep = (ctypes.c_uint32 * 40)()
+    check(load().nxb_selftest_numerics(ctypes.cast(rep, ctypes.c_void_p), 40), "nxb_selftest_numerics")
+    return list(rep)
+
+
+def version() -> str:
+    return load().nxb_version().decode()

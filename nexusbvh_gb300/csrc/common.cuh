@@ -1,0 +1,177 @@
+// common.cuh - shared device-side definitions of the GB300 BVH builder.
+//
+// Numerics: the whole library is compiled with --use_fast_math, the flag
+// the reference builds with (NexusBVH/CMakeLists.txt:46-59), so float
+// add/sub/mul/min/max flush subnormals and `/` is the fast-math divide.
+// Expressions whose rounding decides topology are written with explicit
+// intrinsics so that they do not depend on the compiler's contraction
+// choices; the self-test (nxb_selftest_numerics) checks them against the
+// plain source expressions the reference uses.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/nxb_gb300.h"
+
+namespace nxb {
+
+constexpr uint32_t kInvalid = 0xFFFFFFFFu;
+constexpr uint32_t kFullMask = 0xFFFFFFFFu;
+
+// Upper bound on polls of a cross-CTA flag before a kernel gives up, sets
+// its error word and returns (polls back off with __nanosleep, so this is
+// well under a second of waiting on GB300).
+constexpr uint32_t kSpinLimit = 1u << 20;
+
+struct Box {
+    float3 mn;
+    float3 mx;
+};
+
+struct __align__(16) Node2 {
+    Box b;
+    uint32_t left;
+    uint32_t right;
+};
+static_assert(sizeof(Node2) == 32, "BVH2 node layout");
+
+struct __align__(16) Node8 {
+    float p[3];
+    uint8_t e[3];
+    uint8_t imask;
+    uint32_t child_base;
+    uint32_t prim_base;
+    uint8_t meta[8];
+    uint8_t qlo[3][8];
+    uint8_t qhi[3][8];
+};
+static_assert(sizeof(Node8) == 80, "BVH8 node layout");
+
+// ------------------------------------------------------------ float helpers
+__device__ __forceinline__ float3 fmin3(float3 a, float3 b) {
+    return make_float3(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z));
+}
+__device__ __forceinline__ float3 fmax3(float3 a, float3 b) {
+    return make_float3(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z));
+}
+__device__ __forceinline__ void grow(Box& self, const Box& other) {
+    self.mn = fmin3(self.mn, other.mn);
+    self.mx = fmax3(self.mx, other.mx);
+}
+
+// Surface area / 2 of a box: dx*dy + dy*dz + dz*dx with the reference's
+// rounding, fma(dz, dx, fma(dx, dy, dy*dz)) (pinned by the self-test).
+__device__ __forceinline__ float half_area(const Box& b) {
+    float dx = b.mx.x - b.mn.x;
+    float dy = b.mx.y - b.mn.y;
+    float dz = b.mx.z - b.mn.z;
+    return __fmaf_rn(dz, dx, __fmaf_rn(dx, dy, dy * dz));
+}
+
+// Float <-> monotone uint32 (for atomicMin/Max on floats without CAS
+// loops); -0 orders below +0.
+__device__ __forceinline__ uint32_t f2ord(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+// ------------------------------------------------------------ Morton
+// Spread the low 10 / 21 bits of x three bits apart (magic-number form).
+__device__ __forceinline__ uint32_t spread3_10(uint32_t x) {
+    x &= 0x3FFu;
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+__device__ __forceinline__ uint64_t spread3_21(uint64_t x) {
+    x &= 0x1FFFFFull;
+    x = (x | (x << 32)) & 0x001F00000000FFFFull;
+    x = (x | (x << 16)) & 0x001F0000FF0000FFull;
+    x = (x | (x << 8)) & 0x100F00F00F00F00Full;
+    x = (x | (x << 4)) & 0x10C30C30C30C30C3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+// ------------------------------------------------------------ memory ops
+__device__ __forceinline__ uint64_t ld_relaxed_u64(const uint64_t* p) {
+    uint64_t v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(uint64_t* p, uint64_t v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t atom_exch_acq_rel(uint32_t* p, uint32_t v) {
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.exch.b32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+// Box of a BVH2 node read through L2 (data written by other CTAs).
+__device__ __forceinline__ Box load_box_cg(const Node2* nodes, uint32_t i) {
+    const float4* p = reinterpret_cast<const float4*>(nodes + i);
+    float4 a = __ldcg(p);
+    float2 b = __ldcg(reinterpret_cast<const float2*>(p + 1));
+    Box r;
+    r.mn = make_float3(a.x, a.y, a.z);
+    r.mx = make_float3(a.w, b.x, b.y);
+    return r;
+}
+__device__ __forceinline__ Box load_box(const Node2* nodes, uint32_t i) {
+    const float4* p = reinterpret_cast<const float4*>(nodes + i);
+    float4 a = __ldg(p);
+    float2 b = __ldg(reinterpret_cast<const float2*>(p + 1));
+    Box r;
+    r.mn = make_float3(a.x, a.y, a.z);
+    r.mx = make_float3(a.w, b.x, b.y);
+    return r;
+}
+__device__ __forceinline__ void store_node(Node2* nodes, uint32_t i, const Box& b, uint32_t l, uint32_t r) {
+    float4* p = reinterpret_cast<float4*>(nodes + i);
+    p[0] = make_float4(b.mn.x, b.mn.y, b.mn.z, b.mx.x);
+    p[1] = make_float4(b.mx.y, b.mx.z, __uint_as_float(l), __uint_as_float(r));
+}
+
+__device__ __forceinline__ Box shfl_box(const Box& b, uint32_t src) {
+    Box r;
+    r.mn.x = __shfl_sync(kFullMask, b.mn.x, src);
+    r.mn.y = __shfl_sync(kFullMask, b.mn.y, src);
+    r.mn.z = __shfl_sync(kFullMask, b.mn.z, src);
+    r.mx.x = __shfl_sync(kFullMask, b.mx.x, src);
+    r.mx.y = __shfl_sync(kFullMask, b.mx.y, src);
+    r.mx.z = __shfl_sync(kFullMask, b.mx.z, src);
+    return r;
+}
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+__device__ __forceinline__ void set_error(uint32_t* err, uint32_t bit) {
+    if (err) atomicOr(err, bit);
+}
+
+}  // namespace nxb

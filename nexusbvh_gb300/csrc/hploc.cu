@@ -1,0 +1,209 @@
+// hploc.cu - stage 4: H-PLOC binary BVH (Benthin et al. 2024).
+//
+// Replaces BuildBVH2Kernel (NexusBVH/src/Cuda/BinaryBuilder.cu:200-273).
+// The decisions are the reference's, so the topology and every box are
+// identical; how they are computed on the GPU differs:
+//   * the bottom-up LBVH climb (Apetrei 2014; FindParentId/Delta,
+//     BinaryBuilder.cu:14-40) hands ranges over with acquire/release
+//     exchanges, and cross-CTA data is read through L2 (the reference reads
+//     node boxes with plain, L1-cacheable loads);
+//   * LoadIndices (:42-57) loads the left and right windows of 16 cluster
+//     ids in one round trip (lanes 0-15 and 16-31) and packs them with one
+//     shuffle, instead of two dependent loads;
+//   * FindNearestNeighbor (:126-163) is evaluated as what it computes: for
+//     lane i, the first minimum of the union area (compared as uint32 bit
+//     patterns) over candidates i+1, i-1, i+2, i-2, ..., i+R, i-R.  Each
+//     pair's area is computed once and sent back to the partner with one
+//     shuffle (7 shuffles per radius step instead of 10);
+//   * the merge, node numbering by one atomicAdd per warp, and the
+//     order-preserving compaction follow MergeClustersCreateBVH2Node
+//     (:71-124).
+// A window whose valid ids are not a prefix (impossible for a correct
+// climb) sets NXB_DEVERR_HPLOC_INVALID_CLUSTER instead of reading out of
+// bounds.
+#include "pipeline.h"
+
+namespace nxb {
+namespace {
+
+constexpr int kThreads = 128;
+constexpr uint32_t kMergeThreshold = 16;  // MERGING_THRESHOLD, BinaryBuilder.cu:10
+
+__device__ __forceinline__ uint64_t delta(const uint32_t* k, uint32_t a, uint32_t b) {
+    return (((uint64_t)__ldg(k + a) << 32) | a) ^ (((uint64_t)__ldg(k + b) << 32) | b);
+}
+__device__ __forceinline__ uint64_t delta(const uint64_t* k, uint32_t a, uint32_t b) {
+    const uint64_t d = __ldg(k + a) ^ __ldg(k + b);
+    return d ? d : (uint64_t)(a ^ b);
+}
+
+template <int R>
+__device__ __forceinline__ uint32_t nearest_neighbour(uint32_t num, const Box& cb) {
+    const uint32_t lane = lane_id();
+    uint32_t best = kInvalid, best_idx = kInvalid;
+#pragma unroll
+    for (uint32_t r = 1; r <= (uint32_t)R; ++r) {
+        Box nb = shfl_box(cb, (lane + r) & 31u);
+        uint32_t a = kInvalid;
+        if (lane + r < num) {
+            grow(nb, cb);
+            a = __float_as_uint(half_area(nb));
+        }
+        const uint32_t back = __shfl_sync(kFullMask, a, (lane - r) & 31u);
+        if (a < best) {
+            best = a;
+            best_idx = lane + r;
+        }
+        if (back < best) {
+            best = back;
+            best_idx = lane - r;
+        }
+    }
+    return best_idx;
+}
+
+struct MergeCtx {
+    Node2* nodes;
+    uint32_t* counter;
+    uint32_t node_limit;
+    uint32_t* err;
+};
+
+__device__ __forceinline__ uint32_t merge_step(const MergeCtx& m, uint32_t num, uint32_t nn, uint32_t& cid, Box& cb) {
+    const uint32_t lane = lane_id();
+    const uint32_t nn_of_nn = __shfl_sync(kFullMask, nn, nn & 31u);
+    const bool mutual = lane < num && lane == nn_of_nn;
+    const bool merge = mutual && lane < nn;
+    const uint32_t mmask = __ballot_sync(kFullMask, merge);
+    const uint32_t mcount = __popc(mmask);
+    uint32_t base = 0;
+    if (lane == 0 && mcount) base = atomicAdd(m.counter, mcount);
+    base = __shfl_sync(kFullMask, base, 0);
+    const uint32_t ncid = __shfl_sync(kFullMask, cid, nn & 31u);
+    const Box nb = shfl_box(cb, nn & 31u);
+    if (merge) {
+        grow(cb, nb);
+        const uint32_t idx = base + __popc(mmask & lanemask_lt());
+        if (idx < m.node_limit) {
+            store_node(m.nodes, idx, cb, cid, ncid);
+        } else {
+            set_error(m.err, NXB_DEVERR_HPLOC_INVALID_CLUSTER);
+        }
+        cid = idx;
+    }
+    const uint32_t vmask = __ballot_sync(kFullMask, merge || !mutual);
+    const int sh = __fns(vmask, 0, lane + 1);
+    cid = __shfl_sync(kFullMask, cid, (uint32_t)sh & 31u);
+    cb = shfl_box(cb, (uint32_t)sh & 31u);
+    if (sh < 0) cid = kInvalid;
+    return num - mcount;
+}
+
+template <int R>
+__device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t right, uint32_t split, bool final,
+                                        uint32_t* cluster, const MergeCtx& m) {
+    const uint32_t lane = lane_id();
+    const uint32_t l_start = __shfl_sync(kFullMask, left, owner);
+    const uint32_t r_end = __shfl_sync(kFullMask, right, owner) + 1;
+    const uint32_t mid = __shfl_sync(kFullMask, split, owner);
+    const bool fin = __shfl_sync(kFullMask, final ? 1u : 0u, owner) != 0;
+
+    const uint32_t l_size = min(mid - l_start, kMergeThreshold);
+    const uint32_t r_size = min(r_end - mid, kMergeThreshold);
+    uint32_t v = kInvalid;
+    if (lane < 16) {
+        if (lane < l_size) v = __ldcg(cluster + l_start + lane);
+    } else if (lane - 16 < r_size) {
+        v = __ldcg(cluster + mid + lane - 16);
+    }
+    const uint32_t vb = __ballot_sync(kFullMask, v != kInvalid);
+    const uint32_t num_left = __popc(vb & 0xFFFFu), num_right = __popc(vb >> 16);
+    if ((vb & 0xFFFFu) != ((1u << num_left) - 1u) || (vb >> 16) != ((1u << num_right) - 1u)) {
+        if (lane == 0) set_error(m.err, NXB_DEVERR_HPLOC_INVALID_CLUSTER);
+        return;
+    }
+    uint32_t num = num_left + num_right;
+    const uint32_t src = lane < num_left ? lane : 16u + lane - num_left;
+    uint32_t cid = __shfl_sync(kFullMask, v, src & 31u);
+    if (lane >= num) cid = kInvalid;
+    if (__ballot_sync(kFullMask, lane < num && cid >= m.node_limit)) {
+        if (lane == 0) set_error(m.err, NXB_DEVERR_HPLOC_INVALID_CLUSTER);
+        return;
+    }
+    Box cb;
+    if (lane < num) {
+        cb = load_box_cg(m.nodes, cid);
+    } else {
+        cb.mn = make_float3(0.f, 0.f, 0.f);
+        cb.mx = cb.mn;
+    }
+    const uint32_t threshold = fin ? 1u : kMergeThreshold;
+    while (num > threshold) {
+        const uint32_t nn = nearest_neighbour<R>(num, cb);
+        num = merge_step(m, num, nn, cid, cb);
+    }
+    if (lane < num_left + num_right) __stcg(cluster + l_start + lane, cid);
+    __threadfence();
+}
+
+template <typename K, int R>
+__global__ __launch_bounds__(kThreads) void hploc_kernel(const K* __restrict__ keys, uint32_t* cluster,
+                                                         uint32_t* parent, Node2* nodes, uint32_t n,
+                                                         uint32_t* counter, uint32_t* err) {
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t left = idx, right = idx, split = 0;
+    bool active = idx < n;
+    MergeCtx m{nodes, counter, 2 * n - 1, err};
+    while (__ballot_sync(kFullMask, active)) {
+        if (active) {
+            uint32_t prev;
+            const bool go_right =
+                left == 0 || (right != n - 1 && delta(keys, right, right + 1) < delta(keys, left - 1, left));
+            if (go_right) {
+                prev = atom_exch_acq_rel(parent + right, left);
+                if (prev != kInvalid) {
+                    split = right + 1;
+                    right = prev;
+                }
+            } else {
+                prev = atom_exch_acq_rel(parent + left - 1, right);
+                if (prev != kInvalid) {
+                    split = left;
+                    left = prev;
+                }
+            }
+            if (prev == kInvalid) active = false;
+        }
+        const uint32_t size = right - left + 1;
+        const bool final = active && size == n;
+        uint32_t todo = __ballot_sync(kFullMask, active && (size > kMergeThreshold || final));
+        while (todo) {
+            const uint32_t owner = __ffs(todo) - 1;
+            ploc_merge<R>(owner, left, right, split, final, cluster, m);
+            todo &= todo - 1;
+        }
+    }
+}
+
+template <typename K>
+cudaError_t launch_t(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, uint32_t n, uint32_t radius,
+                     uint32_t* counter, uint32_t* err, cudaStream_t s) {
+    const uint32_t grid = (n + kThreads - 1) / kThreads;
+    switch (radius) {
+        case 4: hploc_kernel<K, 4><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, n, counter, err); break;
+        case 16: hploc_kernel<K, 16><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, n, counter, err); break;
+        default: hploc_kernel<K, 8><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, n, counter, err); break;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
+                         uint32_t n, uint32_t radius, uint32_t* counter, uint32_t* err, cudaStream_t s) {
+    if (key_bytes == 4)
+        return launch_t<uint32_t>((const uint32_t*)keys, cluster_idx, parent, nodes, n, radius, counter, err, s);
+    return launch_t<uint64_t>((const uint64_t*)keys, cluster_idx, parent, nodes, n, radius, counter, err, s);
+}
+
+}  // namespace nxb

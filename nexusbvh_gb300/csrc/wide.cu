@@ -1,0 +1,341 @@
+// wide.cu - stage 5: BVH2 -> compressed 8-wide BVH (Ylitie et al. 2017).
+//
+// Replaces BuildBVH8Kernel (NexusBVH/src/Cuda/WideConverter.cu:225-414).
+// The reference launches one thread per work slot (n threads) and keeps
+// every CTA spinning in lock-step on __syncthreads_count until its slots
+// are filled.  Here a persistent grid (sized to the SM count) claims
+// batches of 32 slots in increasing order; a warp polls its batch with
+// bounded relaxed loads and processes whichever lanes are ready, so no
+// resident warp ever waits on a warp that has not started.  The three
+// allocation counters are bumped once per warp iteration with a warp scan
+// instead of once per node.  The decisions are the reference's:
+//   * expansion always re-opens the highest-indexed inner child, the child
+//     with the smaller area going to the re-opened position (:284-330);
+//   * greedy slot assignment in child order, first strictly best slot
+//     (GreedyAssignment, :104-153);
+//   * node encoding with 8-bit quantised child boxes (CreateBVH8Node,
+//     :156-206; CeilLog2/InvPow2, BuilderUtils.h:335-347);
+//   * the one-primitive tree special case (CreateBVH8SingleLeaf, :209-222).
+#include <algorithm>
+
+#include "pipeline.h"
+
+namespace nxb {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr float kQuantStep = 1.0f / 255.0f;  // 1/((1<<NQ)-1), NQ = 8
+constexpr uint32_t kQueueSpinLimit = 1u << 20;
+
+__device__ __forceinline__ uint32_t nib(uint32_t x, uint32_t i) { return (x >> (4 * i)) & 0xFu; }
+__device__ __forceinline__ uint32_t popc_below(uint32_t m, uint32_t i) { return __popc(m & ((1u << i) - 1u)); }
+
+__device__ __forceinline__ uint32_t ceil_log2_biased(float x) {
+    const uint32_t ix = __float_as_uint(x);
+    const uint32_t ex = (ix >> 23) & 0xFFu;
+    return ex + ((ix & 0x7FFFFFu) != 0 ? 1u : 0u);
+}
+__device__ __forceinline__ float inv_pow2(uint8_t e) { return __uint_as_float((uint32_t)(254 - (int)e) << 23); }
+
+__device__ __forceinline__ Node2 load_node(const Node2* b2, uint32_t i) {
+    const uint4* p = reinterpret_cast<const uint4*>(b2 + i);
+    const uint4 a = __ldg(p), b = __ldg(p + 1);
+    Node2 r;
+    r.b.mn = make_float3(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z));
+    r.b.mx = make_float3(__uint_as_float(a.w), __uint_as_float(b.x), __uint_as_float(b.y));
+    r.left = b.z;
+    r.right = b.w;
+    return r;
+}
+
+// GetCost (WideConverter.cu:25-30): sign pattern of slot s applied to the
+// parent-to-child centroid offset.
+__device__ __forceinline__ float slot_cost(uint32_t s, float3 o) {
+    return ((s >> 2) & 1 ? -1.0f : 1.0f) * o.x + ((s >> 1) & 1 ? -1.0f : 1.0f) * o.y + (s & 1 ? -1.0f : 1.0f) * o.z;
+}
+
+__device__ __forceinline__ uint32_t greedy_assign(float3 pc, const uint32_t* child, uint32_t count,
+                                                  const Node2* b2) {
+    uint32_t asg = kInvalid;
+    for (uint32_t c = 0; c < count; ++c) {
+        const Box cb = load_box(b2, child[c]);
+        const float3 off = make_float3(pc.x - (cb.mx.x + cb.mn.x), pc.y - (cb.mx.y + cb.mn.y),
+                                       pc.z - (cb.mx.z + cb.mn.z));
+        float best = -3.402823466e+38f;
+        uint32_t slot = 0xFu;
+#pragma unroll
+        for (uint32_t s = 0; s < 8; ++s) {
+            if (nib(asg, s) != 0xFu) continue;
+            const float cost = slot_cost(s, off);
+            if (cost > best) {
+                best = cost;
+                slot = s;
+            }
+        }
+        if (slot < 8) {
+            asg &= ~(0xFu << (4 * slot));
+            asg |= c << (4 * slot);
+        }
+    }
+    return asg;
+}
+
+__device__ __forceinline__ void write_node8(Node8* dst, const Box& bounds, const uint32_t* child, uint32_t child_base,
+                                            uint32_t prim_base, uint32_t asg, uint32_t inner, uint32_t leaf,
+                                            const Node2* b2) {
+    uint32_t w[20];
+#pragma unroll
+    for (int i = 0; i < 20; ++i) w[i] = 0;
+    const float3 diag = make_float3(bounds.mx.x - bounds.mn.x, bounds.mx.y - bounds.mn.y, bounds.mx.z - bounds.mn.z);
+    const uint8_t ex = (uint8_t)ceil_log2_biased(diag.x * kQuantStep);
+    const uint8_t ey = (uint8_t)ceil_log2_biased(diag.y * kQuantStep);
+    const uint8_t ez = (uint8_t)ceil_log2_biased(diag.z * kQuantStep);
+    const float3 inv = make_float3(inv_pow2(ex), inv_pow2(ey), inv_pow2(ez));
+    w[0] = __float_as_uint(bounds.mn.x);
+    w[1] = __float_as_uint(bounds.mn.y);
+    w[2] = __float_as_uint(bounds.mn.z);
+    uint32_t imask = 0;
+    w[4] = child_base;
+    w[5] = prim_base;
+#pragma unroll
+    for (uint32_t i = 0; i < 8; ++i) {
+        const uint32_t a = nib(asg, i);
+        uint32_t meta;
+        if (inner & (1u << i)) {
+            imask |= 1u << i;
+            meta = 0x20u | (24u + i);
+        } else if (a != 0xFu) {
+            meta = 0x20u | popc_below(leaf, i);
+        } else {
+            continue;
+        }
+        const uint32_t sh = 8u * (i & 3u);
+        w[6 + (i >> 2)] |= meta << sh;
+        const Box cb = load_box(b2, child[a]);
+        const uint32_t qlx = (uint8_t)floorf((cb.mn.x - bounds.mn.x) * inv.x);
+        const uint32_t qly = (uint8_t)floorf((cb.mn.y - bounds.mn.y) * inv.y);
+        const uint32_t qlz = (uint8_t)floorf((cb.mn.z - bounds.mn.z) * inv.z);
+        const uint32_t qhx = (uint8_t)ceilf((cb.mx.x - bounds.mn.x) * inv.x);
+        const uint32_t qhy = (uint8_t)ceilf((cb.mx.y - bounds.mn.y) * inv.y);
+        const uint32_t qhz = (uint8_t)ceilf((cb.mx.z - bounds.mn.z) * inv.z);
+        w[8 + (i >> 2)] |= qlx << sh;
+        w[10 + (i >> 2)] |= qly << sh;
+        w[12 + (i >> 2)] |= qlz << sh;
+        w[14 + (i >> 2)] |= qhx << sh;
+        w[16 + (i >> 2)] |= qhy << sh;
+        w[18 + (i >> 2)] |= qhz << sh;
+    }
+    w[3] = (uint32_t)ex | ((uint32_t)ey << 8) | ((uint32_t)ez << 16) | (imask << 24);
+    uint4* d = reinterpret_cast<uint4*>(dst);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) d[k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+}
+
+__global__ void bvh8_init_kernel(uint64_t* pairs, uint32_t n, uint32_t* ctr) {
+    const uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    for (uint32_t i = i0; i < n; i += gridDim.x * blockDim.x)
+        pairs[i] = i == 0 ? ((uint64_t)(2 * n - 2) << 32) : ~0ull;
+    if (i0 == 0) {
+        ctr[0] = 0;
+        ctr[1] = 1;
+        ctr[2] = 0;
+        ctr[3] = 1;
+    }
+}
+
+__global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict__ b2, uint32_t n, Node8* out,
+                                                        uint32_t cap, uint32_t* prim_idx, uint64_t* pairs,
+                                                        uint32_t* ctr, uint32_t* err) {
+    const uint32_t lane = lane_id();
+    if (n == 1) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            uint32_t child[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            write_node8(out, load_box(b2, 0), child, 0, 0, 0xFFFFFFF0u, 0u, 1u, b2);
+            prim_idx[0] = 0;
+            ctr[2] = 1;
+        }
+        return;
+    }
+    for (;;) {
+        uint32_t batch = 0;
+        if (lane == 0) batch = atomicAdd(ctr, 32u);
+        batch = __shfl_sync(kFullMask, batch, 0);
+        if (batch >= n) return;
+        const uint32_t slot = batch + lane;
+        bool active = slot < n;
+        uint32_t idle = 0;
+        while (__any_sync(kFullMask, active)) {
+            uint64_t pr = 0;
+            bool ready = false;
+            if (active) {
+                pr = ld_relaxed_u64(pairs + slot);
+                ready = (uint32_t)(pr >> 32) != kInvalid;
+            }
+            if (!__any_sync(kFullMask, ready)) {
+                if (++idle > kQueueSpinLimit) {
+                    if (lane == 0) set_error(err, NXB_DEVERR_BVH8_QUEUE_TIMEOUT);
+                    return;
+                }
+                __nanosleep(100);
+                continue;
+            }
+            idle = 0;
+            const uint32_t b2i = (uint32_t)(pr >> 32), b8i = (uint32_t)pr;
+            bool internal = false;
+            Node2 nd;
+            if (ready && b2i >= 2 * n - 1) {
+                set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
+                active = false;
+                ready = false;
+            }
+            if (ready) {
+                nd = load_node(b2, b2i);
+                if (nd.left != kInvalid && (nd.left >= 2 * n - 1 || nd.right >= 2 * n - 1)) {
+                    set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
+                    active = false;
+                } else if (nd.left == kInvalid) {
+                    if (b8i < n)
+                        prim_idx[b8i] = nd.right;
+                    else
+                        set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
+                    active = false;
+                } else {
+                    internal = true;
+                }
+            }
+            uint32_t child[8];
+            uint32_t inner = 0, count = 0, asg = kInvalid, leaf = 0;
+            if (internal) {
+                uint32_t l0 = nd.left, l1 = nd.right;
+                int msb = 0;
+                while (true) {
+                    const Node2 c0 = load_node(b2, l0), c1 = load_node(b2, l1);
+                    uint32_t first = half_area(c0.b) < half_area(c1.b) ? 0u : 1u;
+#pragma unroll
+                    for (uint32_t i = 0; i < 2; ++i) {
+                        const uint32_t idx = i == 0 ? (uint32_t)msb : count;
+                        const Node2& c = first == 0 ? c0 : c1;
+                        if (c.left != kInvalid) inner |= 1u << idx;
+                        child[idx] = first == 0 ? l0 : l1;
+                        count++;
+                        first ^= 1u;
+                    }
+                    msb = 31 - __clz(inner);
+                    if (msb < 0 || count == 8) break;
+                    inner &= ~(1u << msb);
+                    count--;
+                    const Node2 o = load_node(b2, child[msb]);
+                    l0 = o.left;
+                    l1 = o.right;
+                    if (l0 >= 2 * n - 1 || l1 >= 2 * n - 1) {  // corrupt BVH2: stop here, report
+                        set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
+                        break;
+                    }
+                }
+                const float3 pc = make_float3(nd.b.mn.x + nd.b.mx.x, nd.b.mn.y + nd.b.mx.y, nd.b.mn.z + nd.b.mx.z);
+                asg = greedy_assign(pc, child, count, b2);
+                uint32_t ninner = 0;
+#pragma unroll
+                for (uint32_t i = 0; i < 8; ++i) {
+                    const uint32_t a = nib(asg, i);
+                    if (a == 0xFu) continue;
+                    const uint32_t bit = (inner >> a) & 1u;
+                    ninner |= bit << i;
+                    leaf |= (bit ^ 1u) << i;
+                }
+                inner = ninner;
+            }
+            // warp-aggregated allocation of inner nodes, leaves and work slots
+            const uint32_t ic = internal ? (uint32_t)__popc(inner) : 0u;
+            const uint32_t lc = internal ? count - ic : 0u;
+            const uint32_t wc = internal ? count - 1u : 0u;
+            const uint32_t packed = ic | (lc << 10) | (wc << 20);
+            uint32_t incl = packed;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
+                if (lane >= (uint32_t)o) incl += y;
+            }
+            uint32_t bases[3] = {0, 0, 0};
+            if (lane == 31) {
+                const uint32_t tn = incl & 0x3FFu, tl = (incl >> 10) & 0x3FFu, tw = incl >> 20;
+                if (tn) bases[0] = atomicAdd(ctr + 1, tn);
+                if (tl) bases[1] = atomicAdd(ctr + 2, tl);
+                if (tw) bases[2] = atomicAdd(ctr + 3, tw);
+            }
+            const uint32_t nb = __shfl_sync(kFullMask, bases[0], 31);
+            const uint32_t lb = __shfl_sync(kFullMask, bases[1], 31);
+            const uint32_t wb = __shfl_sync(kFullMask, bases[2], 31);
+            if (internal) {
+                const uint32_t excl = incl - packed;
+                const uint32_t child_base = nb + (excl & 0x3FFu);
+                const uint32_t prim_base = lc ? lb + ((excl >> 10) & 0x3FFu) : 0u;
+                const uint32_t work_base = wb + (excl >> 20);
+                if (child_base + ic > cap || work_base + wc > n || b8i >= cap) {
+                    set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
+                    active = false;
+                } else {
+                    const uint32_t occupied = inner | leaf;
+#pragma unroll
+                    for (uint32_t i = 0; i < 8; ++i) {
+                        if (!((occupied >> i) & 1u)) continue;
+                        uint64_t pair = (uint64_t)child[nib(asg, i)] << 32;
+                        pair |= (inner >> i) & 1u ? child_base + popc_below(inner, i) : prim_base + popc_below(leaf, i);
+                        const uint32_t c = popc_below(occupied, i);
+                        st_relaxed_u64(pairs + (c == 0 ? slot : work_base + c - 1), pair);
+                    }
+                    write_node8(out + b8i, nd.b, child, child_base, prim_base, asg, inner, leaf, b2);
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+}  // namespace
+
+// Bounded-wait check: a two-primitive BVH2 whose work queue is never seeded,
+// so every slot poll expires.  Returns the error word.
+cudaError_t run_bvh8_stall_probe(uint32_t* err_out) {
+    const uint32_t n = 2;
+    unsigned char* buf = nullptr;
+    const size_t bytes = 3 * sizeof(Node2) + 2 * sizeof(Node8) + 8 * n + 4 * n + 32;
+    cudaError_t e = cudaMalloc(&buf, bytes);
+    if (e) return e;
+    Node2* b2 = (Node2*)buf;
+    Node8* out = (Node8*)(buf + 3 * sizeof(Node2));
+    uint64_t* pairs = (uint64_t*)(buf + 3 * sizeof(Node2) + 2 * sizeof(Node8));
+    uint32_t* prim = (uint32_t*)(pairs + n);
+    uint32_t* ctr = prim + n;
+    uint32_t* err = ctr + 4;
+    e = cudaMemset(buf, 0, bytes);
+    if (!e) e = cudaMemset(pairs, 0xFF, 8 * n);
+    const uint32_t c[5] = {0, 1, 0, 1, 0};
+    if (!e) e = cudaMemcpy(ctr, c, sizeof(c), cudaMemcpyHostToDevice);
+    if (!e) {
+        bvh8_kernel<<<1, kThreads>>>(b2, n, out, 2, prim, pairs, ctr, err);
+        e = cudaGetLastError();
+    }
+    if (!e) e = cudaMemcpy(err_out, err, 4, cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    return e;
+}
+
+cudaError_t launch_bvh8_init(uint64_t* pairs, uint32_t n, uint32_t* ctr, cudaStream_t s) {
+    uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)device_info().sms * 8);
+    bvh8_init_kernel<<<grid, 256, 0, s>>>(pairs, n, ctr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bvh8(const Node2* bvh2, uint32_t n, Node8* out, uint32_t cap, uint32_t* prim_idx, uint64_t* pairs,
+                        uint32_t* ctr, uint32_t* err, cudaStream_t s) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh8_kernel, kThreads, 0);
+    if (per_sm < 1) per_sm = 1;
+    uint32_t want = (n + kThreads - 1) / kThreads;
+    uint32_t grid = std::max(1u, std::min(want, (uint32_t)(device_info().sms * per_sm)));
+    bvh8_kernel<<<grid, kThreads, 0, s>>>(bvh2, n, out, cap, prim_idx, pairs, ctr, err);
+    return cudaGetLastError();
+}
+
+}  // namespace nxb

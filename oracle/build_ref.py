@@ -1,0 +1,130 @@
+"""Build recipe for the reference's own CUDA build (test infrastructure).
+
+The reference (StokastX/NexusBVH) is a few C++/CUDA translation units with
+no build-time code generation; its only external dependency is CUB, which
+ships inside the CUDA toolkit (CCCL 3.0.1 with CUDA 13.0).  Its CMake build
+is not used: this script compiles the sources directly.
+
+  stage():  copies the reference's source files verbatim from the read-only
+            checkout (default /root/reference, or $NXB_REFERENCE) into
+            oracle/_ref/src/, plus one patched copy of BinaryBuilder.cu whose
+            SEARCH_RADIUS can be set with -D (the reference hard-codes 8).
+            oracle/_ref/ is git-ignored: nothing of the reference is
+            committed.  The staged copy travels with the working tree to the
+            GPU machine, which has no checkout of the reference.
+  build():  compiles the staged sources with the reference's flags
+            (--use_fast_math; arch sm_103, which is what `native` resolves to
+            on GB300) plus oracle/ref_harness.cpp into
+            oracle/_ref/libnxbref_r{4,8,16}.so, one per search radius.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+ORACLE_DIR = Path(__file__).resolve().parent
+REF_OUT = ORACLE_DIR / "_ref"
+STAGE = REF_OUT / "src"
+OBJ = REF_OUT / "obj"
+RADII = (8, 16, 4)
+FILES = [
+    "NexusBVH/include/NXB/AABB.h", "NexusBVH/include/NXB/BVH.h", "NexusBVH/include/NXB/BVHBuilder.h",
+    "NexusBVH/include/NXB/BVHBuildMetrics.h", "NexusBVH/include/NXB/BuildConfig.h",
+    "NexusBVH/include/NXB/Triangle.h", "NexusBVH/include/NXB/Math/CudaMath.h",
+    "NexusBVH/src/BVHBuilder.cpp", "NexusBVH/src/Math/Math.h",
+    "NexusBVH/src/Cuda/BinaryBuilder.cu", "NexusBVH/src/Cuda/BinaryBuilder.h",
+    "NexusBVH/src/Cuda/BuildState.h", "NexusBVH/src/Cuda/BuilderUtils.h", "NexusBVH/src/Cuda/CudaUtils.h",
+    "NexusBVH/src/Cuda/Eval.cu", "NexusBVH/src/Cuda/Eval.h", "NexusBVH/src/Cuda/Setup.cu",
+    "NexusBVH/src/Cuda/Setup.h", "NexusBVH/src/Cuda/WideConverter.cu", "NexusBVH/src/Cuda/WideConverter.h",
+]
+ARCH = ["-gencode", "arch=compute_103,code=sm_103"]
+
+
+def reference_root() -> Path:
+    return Path(os.environ.get("NXB_REFERENCE", "/root/reference"))
+
+
+def lib_path(radius: int = 8) -> Path:
+    return REF_OUT / f"libnxbref_r{radius}.so"
+
+
+def stage() -> bool:
+    src = reference_root()
+    if not (src / "NexusBVH").is_dir():
+        return (STAGE / "NexusBVH").is_dir()
+    for f in FILES:
+        dst = STAGE / f
+        dst.parent.mkdir(parents=True, exist_ok=True)
+        if not dst.exists() or dst.read_bytes() != (src / f).read_bytes():
+            shutil.copyfile(src / f, dst)
+    bb = (src / "NexusBVH/src/Cuda/BinaryBuilder.cu").read_text()
+    patched = bb.replace("#define SEARCH_RADIUS 8", "#ifndef SEARCH_RADIUS\n#define SEARCH_RADIUS 8\n#endif", 1)
+    if patched == bb:
+        raise RuntimeError("SEARCH_RADIUS definition not found in BinaryBuilder.cu")
+    p = STAGE / "NexusBVH/src/Cuda/BinaryBuilder_radius.cu"
+    if not p.exists() or p.read_text() != patched:
+        p.write_text(patched)
+    return True
+
+
+def _run(cmd):
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError(f"reference build step failed: {' '.join(map(str, cmd))}\n{proc.stderr[-4000:]}")
+
+
+def _nvcc() -> str:
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if c and Path(c).exists():
+            return c
+    raise RuntimeError("nvcc not found")
+
+
+def build(force: bool = False) -> list[Path]:
+    if not stage():
+        return []
+    nvcc = _nvcc()
+    OBJ.mkdir(parents=True, exist_ok=True)
+    inc = ["-I", str(STAGE / "NexusBVH/include"), "-I", str(STAGE / "NexusBVH/src")]
+    cu = [nvcc, *ARCH, "--use_fast_math", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", *inc]
+    units = {
+        "BVHBuilder.o": ["g++", "-O2", "-std=c++17", "-fPIC", *inc, "-I/usr/local/cuda/include", "-c",
+                         str(STAGE / "NexusBVH/src/BVHBuilder.cpp")],
+        "Setup.o": cu + ["-c", str(STAGE / "NexusBVH/src/Cuda/Setup.cu")],
+        "WideConverter.o": cu + ["-c", str(STAGE / "NexusBVH/src/Cuda/WideConverter.cu")],
+        "Eval.o": cu + ["-c", str(STAGE / "NexusBVH/src/Cuda/Eval.cu")],
+        "harness.o": ["g++", "-O2", "-std=c++17", "-fPIC", *inc, "-I/usr/local/cuda/include", "-c",
+                      str(ORACLE_DIR / "ref_harness.cpp")],
+        "BinaryBuilder_r8.o": cu + ["-c", str(STAGE / "NexusBVH/src/Cuda/BinaryBuilder.cu")],
+    }
+    for r in RADII:
+        if r != 8:
+            units[f"BinaryBuilder_r{r}.o"] = cu + [f"-DSEARCH_RADIUS={r}", "-c",
+                                                   str(STAGE / "NexusBVH/src/Cuda/BinaryBuilder_radius.cu")]
+    jobs = []
+    for name, cmd in units.items():
+        out = OBJ / name
+        srcs = [Path(a) for a in cmd if a.endswith((".cu", ".cpp"))]
+        if force or not out.exists() or any(s.stat().st_mtime > out.stat().st_mtime for s in srcs):
+            jobs.append(cmd + ["-o", str(out)])
+    if jobs:
+        with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
+            list(ex.map(_run, jobs))
+    libs = []
+    common = [OBJ / n for n in ("BVHBuilder.o", "Setup.o", "WideConverter.o", "Eval.o", "harness.o")]
+    for r in RADII:
+        lib = lib_path(r)
+        objs = common + [OBJ / f"BinaryBuilder_r{r}.o"]
+        if force or jobs or not lib.exists():
+            _run([nvcc, *ARCH, "-shared", "-cudart", "shared", "-o", str(lib), *map(str, objs),
+                  "-Xlinker", "-rpath,/usr/local/cuda/lib64"])
+        libs.append(lib)
+    return libs
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv))

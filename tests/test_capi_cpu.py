@@ -1,0 +1,96 @@
+"""CPU-side checks of the C ABI library: it loads without a GPU, exports every
+entry point include/nxb_gb300.h declares, validates arguments before touching
+the device, and its struct layouts match the reference's."""
+import ctypes
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+import nexusbvh_gb300 as nxb
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "nxb_gb300.h"
+
+
+def declared_functions():
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    return sorted(set(re.findall(r"\b(nxb_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from nexusbvh_gb300 import _build
+    _build.build_cuda()
+    return nxb.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    out = subprocess.run(["nm", "-D", "--defined-only", str(nxb.lib_path())], capture_output=True, text=True).stdout
+    for n in names:
+        assert re.search(rf"\bT {n}$", out, flags=re.M), n
+
+
+def test_status_strings_and_version(lib):
+    for code, name in nxb.STATUS_NAMES.items():
+        assert lib.nxb_status_string(code).decode() == name
+    assert "sm_103a" in nxb.version()
+
+
+def test_argument_checks_need_no_device(lib):
+    out = nxb.CBVH8()
+    c = nxb.BuildConfig().to_c()
+    assert lib.nxb_build_bvh8(None, 1, 10, ctypes.byref(c), None, ctypes.byref(out), None) == 1
+    assert lib.nxb_build_bvh8(16, 1, 0, ctypes.byref(c), None, ctypes.byref(out), None) == 1
+    assert lib.nxb_build_bvh8(16, 7, 10, ctypes.byref(c), None, ctypes.byref(out), None) == 1
+    assert lib.nxb_build_bvh8(16, 1, 1 << 31, ctypes.byref(c), None, ctypes.byref(out), None) == 2
+    bad = nxb.BuildConfig(search_radius=5).to_c()
+    assert lib.nxb_build_bvh8(16, 1, 10, ctypes.byref(bad), None, ctypes.byref(out), None) == 2
+    assert lib.nxb_build_bvh8(16, 1, 10, ctypes.byref(c), None, None, None) == 1
+
+
+def test_workspace_sizes(lib):
+    s = nxb.CSizes()
+    for bits, kb in ((30, 4), (63, 8)):
+        cfg = nxb.BuildConfig(prioritize_speed=bits == 30).to_c()
+        n = 12_582_912
+        assert lib.nxb_query_build_sizes(n, ctypes.byref(cfg), ctypes.byref(s)) == 0
+        assert s.bvh2_node_count == 2 * n - 1
+        assert s.bvh8_node_capacity == (4 * n - 1 + 6) // 7
+        # keys x2, values x2, parent slots, BVH8 work slots, look-back
+        assert s.workspace_bytes >= n * (2 * kb + 8 + 4 + 8)
+        assert s.workspace_bytes < n * (2 * kb + 8 + 4 + 8 + 8)
+    assert lib.nxb_query_build_sizes(0, None, ctypes.byref(s)) == 1
+
+
+def test_struct_layouts():
+    assert ctypes.sizeof(nxb.CAABB) == 24
+    assert ctypes.sizeof(nxb.CBVH2) == 40 and ctypes.sizeof(nxb.CBVH8) == 56
+    assert nxb.CBVH8.prim_idx.offset == 16 and nxb.CBVH8.bounds.offset == 28
+    assert nxb.BVH2_NODE_DTYPE.itemsize == 32 and nxb.BVH8_NODE_DTYPE.itemsize == 80
+    assert nxb.BVH8_NODE_DTYPE.fields["meta"][1] == 24 and nxb.BVH8_NODE_DTYPE.fields["qhi"][1] == 56
+
+
+def test_cpp_facade_compiles(tmp_path):
+    src = tmp_path / "use.cpp"
+    src.write_text(
+        '#include "NXB/BVHBuilder.h"\n'
+        "static_assert(sizeof(NXB::BVH2::Node) == 32, \"\");\n"
+        "static_assert(sizeof(NXB::BVH8::Node) == 80, \"\");\n"
+        "static_assert(sizeof(NXB::BVH8::NodeExplicit) == 80, \"\");\n"
+        "static_assert(sizeof(NXB::Triangle) == 36, \"\");\n"
+        "static_assert(sizeof(NXB::BVH2) == 40 && sizeof(NXB::BVH8) == 56, \"\");\n"
+        "NXB::BVH8 f(NXB::Triangle* t, uint32_t n) {\n"
+        "  NXB::BuildConfig c; c.prioritizeSpeed = true;\n"
+        "  NXB::BVHBuildMetrics m;\n"
+        "  return NXB::BuildBVH8<NXB::Triangle>(t, n, c, &m);\n"
+        "}\n"
+        "NXB::BVH2 g(NXB::AABB* b, uint32_t n) { return NXB::BuildBVH2(b, n); }\n")
+    proc = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", f"-I{ROOT / 'include'}", "-I/usr/local/cuda/include",
+                           str(src)], capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr

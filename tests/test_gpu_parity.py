@@ -1,0 +1,224 @@
+"""Parity of the CUDA pipeline with the CPU oracle, stage by stage, through
+the C ABI.  Each stage is fed the GPU output of the previous stage, so every
+comparison isolates one kernel:
+  bounds/leaves   bit-exact
+  Morton codes    bit-exact except where the fast-math divide and the
+                  oracle's IEEE divide land on opposite sides of a
+                  quantisation step (checked: +-1 in that axis only, at a
+                  boundary)
+  sort            keys and permutation bit-exact
+  H-PLOC BVH2     canonical topology + every box bit-exact
+  BVH8            canonical structure, every node byte (except base indices)
+  costs           within 0.1%
+"""
+import numpy as np
+import pytest
+
+import nexusbvh_gb300 as nxb
+from nexusbvh_gb300 import scenes
+from tests import stages as S
+
+pytestmark = pytest.mark.gpu
+
+
+def deinterleave(keys: np.ndarray, key_bits: int) -> np.ndarray:
+    per = 10 if key_bits == 30 else 21
+    k = keys.astype(np.uint64)
+    q = np.zeros((keys.shape[0], 3), dtype=np.uint64)
+    for b in range(per):
+        for a in range(3):
+            q[:, a] |= ((k >> np.uint64(3 * b + a)) & np.uint64(1)) << np.uint64(b)
+    return q.astype(np.int64)
+
+
+def check_morton(keys_g, leaves, scene, key_bits, orc):
+    keys_o = orc.morton(leaves, scene, key_bits)
+    diff = np.nonzero(keys_g != keys_o)[0]
+    if diff.size == 0:
+        return 0
+    qg = deinterleave(keys_g[diff], key_bits)
+    q_o, prod = orc.morton_quantised(leaves[diff], scene, key_bits)
+    q_o = q_o.astype(np.int64)
+    d = qg - q_o
+    assert np.abs(d).max() <= 1, "Morton quantisation differs by more than one step"
+    # every differing axis must sit at a quantisation boundary
+    p = prod.astype(np.float64)
+    boundary = np.where(d > 0, q_o + 1, q_o).astype(np.float64)
+    dist = np.abs(p - boundary)
+    tol = np.maximum(np.abs(p), 1.0) * 2.0 ** -20
+    bad = (d != 0) & (dist > tol)
+    assert not bad.any(), f"{int(bad.sum())} Morton differences away from a quantisation boundary"
+    return int(diff.size)
+
+
+CASES = [
+    ("soup65k-30", lambda: scenes.uniform_soup(65536, seed=0), 30),
+    ("soup65k-63", lambda: scenes.uniform_soup(65536, seed=0), 63),
+    ("sphere64k-30", lambda: scenes.displaced_sphere(256, 128, seed=1), 30),
+    ("sphere64k-63", lambda: scenes.displaced_sphere(256, 128, seed=1), 63),
+    ("clustered100k-63", lambda: scenes.clustered(100_000, seed=2), 63),
+    ("aabb50k-63", lambda: scenes.to_boxes(scenes.clustered(50_000, seed=5)), 63),
+    ("aabb50k-30", lambda: scenes.to_boxes(scenes.uniform_soup(50_000, seed=7)), 30),
+]
+
+
+def run_chain(prims, key_bits, orc, radius=8):
+    n = prims.shape[0]
+    d_nodes, d_scene = S.stage_bounds(prims)
+    leaves_g = S.nodes2(d_nodes)[:n]
+    scene_g = S.host(d_scene)
+    leaves_o, scene_o = orc.scene_bounds(prims)
+    assert leaves_g.tobytes() == leaves_o.tobytes(), "leaf boxes differ"
+    np.testing.assert_array_equal(scene_g, scene_o)
+
+    d_keys = S.stage_morton(d_nodes, d_scene, n, key_bits)
+    keys_g = S.host(d_keys).view(np.uint32 if key_bits == 30 else np.uint64)
+    morton_diffs = check_morton(keys_g, leaves_o, scene_o, key_bits, orc)
+
+    begin, end = (2, 32) if key_bits == 30 else (1, 64)
+    d_sk, d_perm = S.stage_sort(d_keys, n, key_bits)
+    sk_g = S.host(d_sk).view(keys_g.dtype)
+    perm_g = S.host(d_perm).view(np.uint32)
+    sk_o, perm_o = orc.radix_sort(keys_g, begin, end)
+    np.testing.assert_array_equal(sk_g, sk_o)
+    np.testing.assert_array_equal(perm_g, perm_o)
+
+    d_b2 = S.stage_hploc(d_sk, d_perm, d_nodes, n, key_bits, radius)
+    b2_g = S.nodes2(d_b2)
+    b2_o, root_o, err = orc.hploc(sk_g, perm_g, leaves_g, radius)
+    assert err == 0
+    assert root_o == 2 * n - 2
+    assert orc.compare_bvh2(b2_g, 2 * n - 2, b2_o, root_o, n) == 0, "BVH2 differs from the oracle"
+    errs, rep = orc.validate_bvh2(b2_g, n, 2 * n - 2)
+    assert errs == 0, rep
+
+    b8_g, prim_g, nc, lc = S.stage_bvh8(d_b2, n)
+    b8_o, prim_o, err8 = orc.bvh8(b2_g, n, 2 * n - 2)
+    assert err8 == 0
+    assert nc == b8_o.shape[0] and lc == n
+    assert orc.compare_bvh8(b8_g, prim_g, b8_o, prim_o, n) == 0, "BVH8 differs from the oracle"
+    errs8, rep8 = orc.validate_bvh8(b8_g, prim_g, n, leaves_g)
+    assert errs8 == 0, rep8
+
+    rb = S.root_box(b2_g, 2 * n - 2)
+    c2g, c2o = S.cost_bvh2(d_b2, 2 * n - 1, rb), orc.bvh2_cost(b2_g, rb)
+    c8g, c8o = S.cost_bvh8(b8_g, rb), orc.bvh8_cost(b8_g, rb)
+    assert abs(c2g - c2o) <= 1e-3 * abs(c2o)
+    assert abs(c8g - c8o) <= 1e-3 * abs(c8o)
+    return dict(b2=b2_g, b8=b8_g, prim=prim_g, leaves=leaves_g, morton_diffs=morton_diffs, rep8=rep8,
+                costs=(c2g, c8g))
+
+
+@pytest.mark.parametrize("name,make,key_bits", CASES, ids=[c[0] for c in CASES])
+def test_stage_chain_matches_oracle(gpu, orc, name, make, key_bits):
+    run_chain(make(), key_bits, orc)
+
+
+@pytest.mark.parametrize("radius", [4, 16])
+def test_search_radius(gpu, orc, radius):
+    run_chain(scenes.clustered(60_000, seed=11), 63, orc, radius=radius)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 16, 17, 31, 32, 33, 100, 257, 1000, 4097])
+def test_small_sizes(gpu, orc, n):
+    run_chain(scenes.uniform_soup(n, seed=n), 30, orc)
+    run_chain(scenes.uniform_soup(n, seed=n + 1), 63, orc)
+
+
+def test_degenerate_inputs(gpu, orc):
+    # every triangle identical: all keys equal, ties broken by index
+    t = np.tile(np.array([[0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9]], np.float32), (3000, 1))
+    run_chain(t, 30, orc)
+    run_chain(t, 63, orc)
+    # zero extent on one axis (0/0 in the normalisation)
+    f = scenes.uniform_soup(5000, seed=3)
+    f[:, 2::3] = 0.25
+    run_chain(f, 63, orc)
+    # signed zeros and coordinates on the axes
+    z = scenes.displaced_sphere(64, 32, seed=4)
+    z[::7, 0] = -0.0
+    z[::5, 3] = 0.0
+    run_chain(z, 30, orc)
+
+
+def test_pipeline_entry_points_agree(gpu, orc):
+    """nxb_build_async, nxb_build_bvh8 / nxb_build_bvh2 and the stage chain
+    produce the same trees; metrics are filled like the reference's."""
+    prims = scenes.clustered(80_000, seed=9)
+    n = prims.shape[0]
+    chain = run_chain(prims, 63, orc)
+    out = S.build_async(prims, 63)
+    b2 = S.nodes2(out.bvh2.nodes.view(-1))
+    assert orc.compare_bvh2(b2, 2 * n - 2, chain["b2"], 2 * n - 2, n) == 0
+    b8 = S.host(out.nodes.reshape(-1)).view(nxb.BVH8_NODE_DTYPE)
+    prim = S.host(out.prim_idx).view(np.uint32)
+    assert orc.compare_bvh8(b8, prim, chain["b8"], chain["prim"], n) == 0
+
+    m = nxb.BVHBuildMetrics()
+    plain = nxb.build_bvh8(S.dev(prims), nxb.BuildConfig(), m)
+    b8p = S.host(plain.nodes.reshape(-1)).view(nxb.BVH8_NODE_DTYPE)
+    assert orc.compare_bvh8(b8p, S.host(plain.prim_idx).view(np.uint32), chain["b8"], chain["prim"], n) == 0
+    assert m.total_time > 0 and m.bvh8_conversion_time > 0
+    assert abs(m.bvh2_cost - chain["costs"][0]) <= 1e-3 * chain["costs"][0]
+    assert abs(m.bvh8_cost - chain["costs"][1]) <= 1e-3 * chain["costs"][1]
+    assert abs(m.average_child_per_node - (n + plain.node_count - 1) / plain.node_count) < 1e-5
+
+    p2 = nxb.build_bvh2(S.dev(prims), nxb.BuildConfig())
+    assert p2.node_count == 2 * n - 1
+    assert orc.compare_bvh2(S.nodes2(p2.nodes.view(-1)), 2 * n - 2, chain["b2"], 2 * n - 2, n) == 0
+    assert np.allclose(np.array(p2.bounds[0]), chain["b2"][2 * n - 2]["bmin"])
+
+
+def test_numerics_selftest(gpu, orc):
+    rep = nxb.selftest_numerics()
+    assert rep[0] > 0
+    assert rep[3] == 0, "pinned area form differs from the plain expression under --use_fast_math"
+    values = [254.5, 255.0, 255.25, 256.0, 256.5, 300.0, 511.75, -1.5]
+    import math
+    for k, v in enumerate(values):
+        assert rep[4 + k] == orc.load().orc_f2u8(math.floor(v)), f"floor cast of {v}"
+        assert rep[12 + k] == orc.load().orc_f2u8(math.ceil(v)), f"ceil cast of {v}"
+    f = np.array(rep[20:24], dtype=np.uint32).view(np.float32)
+    lib = orc.load()
+    assert np.float32(lib.orc_fmin(0.0, -0.0)).tobytes() == f[0].tobytes()
+    assert np.float32(lib.orc_fmin(-0.0, 0.0)).tobytes() == f[1].tobytes()
+    assert np.float32(lib.orc_fmax(0.0, -0.0)).tobytes() == f[2].tobytes()
+    assert np.float32(lib.orc_fmax(-0.0, 0.0)).tobytes() == f[3].tobytes()
+
+
+def test_bounded_waits_report_errors(gpu):
+    import ctypes
+    words = (ctypes.c_uint32 * 2)()
+    lib = nxb.load()
+    lib.nxb_selftest_bounded_waits.restype = ctypes.c_int
+    lib.nxb_selftest_bounded_waits.argtypes = [ctypes.c_void_p]
+    nxb.check(lib.nxb_selftest_bounded_waits(ctypes.cast(words, ctypes.c_void_p)), "nxb_selftest_bounded_waits")
+    assert words[0] == 0x1 and words[1] == 0x2
+    # the context is still usable
+    run = S.build_async(scenes.uniform_soup(1000, seed=1), 30)
+    assert run.node_count > 0
+
+
+def test_errors_are_status_codes(gpu):
+    import ctypes
+    import torch
+    lib = nxb.load()
+    prims = S.dev(scenes.uniform_soup(1000))
+    b = nxb.Builder()
+    cfg = nxb.BuildConfig()
+    s = b.sizes(1000, cfg)
+    ws = torch.empty(s.workspace_bytes - 256, dtype=torch.uint8, device="cuda")
+    nodes = torch.empty((s.bvh2_node_count, 32), dtype=torch.uint8, device="cuda")
+    res = torch.zeros(64, dtype=torch.uint8, device="cuda")
+    with pytest.raises(nxb.NxbError) as ei:
+        b.enqueue(prims, 1000, cfg, ws, nodes, None, None, res)
+    assert ei.value.status == 5
+    bad = nxb.BuildConfig(search_radius=7)
+    with pytest.raises(nxb.NxbError) as ei:
+        nxb.build_bvh8(prims, bad)
+    assert ei.value.status == 2
+    out = nxb.CBVH8()
+    c = cfg.to_c()
+    assert lib.nxb_build_bvh8(None, 1, 10, ctypes.byref(c), None, ctypes.byref(out), None) == 1
+    assert lib.nxb_build_bvh8(prims.data_ptr(), 1, 0, ctypes.byref(c), None, ctypes.byref(out), None) == 1
+    assert lib.nxb_build_bvh8(prims.data_ptr(), 3, 10, ctypes.byref(c), None, ctypes.byref(out), None) == 1
