@@ -190,6 +190,10 @@ def run_ours(args, world, rank, local):
         enqueue()
     torch.cuda.synchronize()
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(args.steps)]
+    for row in evs:  # torch creates the CUDA event on first record
+        for e in row:
+            e.record(stream)
+    torch.cuda.synchronize()
     ev_arrays = [(ctypes.c_void_p * 6)(*[e.cuda_event for e in row]) for row in evs]
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if world > 1:

@@ -13,7 +13,7 @@ is not used: this script compiles the sources directly.
             committed.  The staged copy travels with the working tree to the
             GPU machine, which has no checkout of the reference.
   build():  compiles the staged sources with the reference's flags
-            (--use_fast_math; arch sm_103, which is what `native` resolves to
+            (--use_fast_math -rdc=true; arch sm_103, which is what `native` resolves to
             on GB300) plus oracle/ref_harness.cpp into
             oracle/_ref/libnxbref_r{4,8,16}.so, one per search radius.
 """
@@ -90,7 +90,7 @@ def build(force: bool = False) -> list[Path]:
     nvcc = _nvcc()
     OBJ.mkdir(parents=True, exist_ok=True)
     inc = ["-I", str(STAGE / "NexusBVH/include"), "-I", str(STAGE / "NexusBVH/src")]
-    cu = [nvcc, *ARCH, "--use_fast_math", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", *inc]
+    cu = [nvcc, *ARCH, "--use_fast_math", "-rdc=true", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", *inc]
     units = {
         "BVHBuilder.o": ["g++", "-O2", "-std=c++17", "-fPIC", *inc, "-I/usr/local/cuda/include", "-c",
                          str(STAGE / "NexusBVH/src/BVHBuilder.cpp")],
