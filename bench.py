@@ -18,10 +18,10 @@ ours:      ``value`` = Mtris/s of nxb_build_async with the triangles resident
            nxb_build_bvh8 with the triangles in pinned host memory: each step
            copies them to the device, builds (allocating outputs), reads the
            result back and frees the BVH.
-reference: the reference's own CUDA build (NXB::BuildBVH8 compiled from its
-           sources into oracle/_ref/) on the same workload; its ``e2e`` adds
-           the host->device copy the same way.  If it is not built, the CPU
-           oracle port stands in (stated in the line).
+reference: the CPU restatement of the reference's algorithm (the oracle
+           port) on all host cores: the reference has no CPU path, and its
+           own CUDA build is not run on the GPU (it faulted; see
+           run_reference).
 Multi-GPU: the build of one mesh does not shard; each rank builds its own
 replica (no collective) and ``value`` = total triangles / max rank time.
 """
@@ -312,80 +312,49 @@ def run_ours(args, world, rank, local):
 
 
 def run_reference(args, world, rank, local):
+    """The reference arm.  The reference's path has no CPU implementation,
+    and its own CUDA build is not run on the GPU any more: its H-PLOC kernel
+    reads cluster ids and node boxes written by other SMs with plain
+    L1-cacheable loads (NexusBVH/src/Cuda/BinaryBuilder.cu:51,185), and it
+    faulted (Xid 31) on the 4,194,304-triangle sphere with 30-bit keys.
+    What is timed here is therefore the CPU restatement of the reference's
+    algorithm (the oracle port) on all host cores, each step one CPU build
+    of a bounded prefix sample of the workload."""
     if rank != 0:
         return
-    import torch
+    import oracle
 
-    torch.cuda.set_device(local)
     prims_np = make_prims(args.workload)
     n = prims_np.shape[0]
     key_bits = args.key_bits
-    line = {"metric": "Mtris/s full build (bounds, Morton, radix sort, H-PLOC BVH2, BVH8)", "unit": "Mtris/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+    m = min(args.cpu_sample, n)
+    sub = np.ascontiguousarray(prims_np[:m])
+    for _ in range(args.warmup):
+        oracle.build(sub[: min(m, 65536)], key_bits, args.radius)
+    times = []
+    stage = np.zeros(5)
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        r = oracle.build(sub, key_bits, args.radius)
+        times.append(time.perf_counter() - t)
+        assert r["err"] == 0
+        stage += np.array(r["stage_ms"])
+    total = sum(times)
+    value = m * args.steps / total / 1e6
+    line = {"metric": "Mtris/s full build (bounds, Morton, radix sort, H-PLOC BVH2, BVH8)", "value": round(value, 3),
+            "unit": "Mtris/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(total / args.steps * 1e3, 2), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "impl": "reference",
             "data": "synthetic (seeded generators standing in for the reference's scene files)",
             "config": {"workload": WORKLOADS[args.workload][0], "n_tris": n, "key_bits": key_bits,
-                       "search_radius": args.radius,
-                       "l2": "inputs larger than L2 (triangles 36 B x n, no flush needed)"}}
-    from oracle import build_ref
-    libp = build_ref.lib_path(args.radius)
-    if not libp.exists():
-        try:
-            build_ref.build()
-        except Exception:
-            pass
-    if not libp.exists():
-        # the reference's own build is unavailable: time the CPU port instead
-        cb = cpu_baseline(prims_np, key_bits, args.radius, args.cpu_sample)
-        line.update(value=cb["value"], ms_per_step=None, cpu_baseline=cb,
-                    e2e={"value": cb["value"], "unit": "Mtris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-                    note="reference CUDA build not available here; the CPU oracle port was timed")
-        print(json.dumps(line), flush=True)
-        return
-    lib = ctypes.CDLL(str(libp))
-    P, U = ctypes.c_void_p, ctypes.c_uint32
-    lib.ref_build_bvh8.argtypes = [P, ctypes.c_int, U, ctypes.c_int, P, P, P, P, P]
-    lib.ref_e2e_bvh8.argtypes = [P, ctypes.c_size_t, P, ctypes.c_int, U, ctypes.c_int, P]
-    ps = 1 if key_bits == 30 else 0
-    d_prims = torch.from_numpy(prims_np).cuda()
-    nc = U(0)
-    for _ in range(args.warmup):
-        assert lib.ref_build_bvh8(d_prims.data_ptr(), 1, n, ps, None, None, ctypes.byref(nc), None, None) == 0
-    # the reference's own definition: sum of its per-stage event times
-    m9 = (ctypes.c_float * 9)()
-    stage = []
-    for _ in range(3):
-        assert lib.ref_build_bvh8(d_prims.data_ptr(), 1, n, ps, None, None, ctypes.byref(nc), None, m9) == 0
-        stage.append(list(m9))
-    stage = np.mean(np.array(stage), axis=0)
-    torch.cuda.synchronize()
-    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clocks:
-        start.record()
-        for _ in range(args.steps):
-            assert lib.ref_build_bvh8(d_prims.data_ptr(), 1, n, ps, None, None, ctypes.byref(nc), None, None) == 0
-        stop.record()
-        torch.cuda.synchronize()
-    elapsed = start.elapsed_time(stop)
-    h = torch.from_numpy(prims_np).pin_memory()
-    e2e_steps = max(3, min(args.steps, 10))
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        assert lib.ref_e2e_bvh8(h.data_ptr(), 36 * n, d_prims.data_ptr(), 1, n, ps, ctypes.byref(nc)) == 0
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    value = n * args.steps / elapsed / 1e3
-    line.update(
-        value=round(value, 2), ms_per_step=round(elapsed / args.steps, 4),
-        e2e={"value": round(n * e2e_steps / e2e_s / 1e6, 2), "unit": "Mtris/s", "h2d_bytes_per_step": 36 * n,
-             "d2h_bytes_per_step": 4, "call": "NXB::BuildBVH8<Triangle> after a pinned host->device copy"},
-        cpu_baseline={"value": round(value, 2), "unit": "Mtris/s", "cores": 0, "kind": "reference",
-                      "sample": "full workload; the reference path is CUDA code on the GPU (host cores only "
-                                "orchestrate); built from its sources with its own flags"},
-        reference_stage_ms={"scene_bounds": float(stage[0]), "morton": float(stage[1]), "radix_sort": float(stage[2]),
-                            "hploc": float(stage[3]), "bvh8": float(stage[4]), "total": float(stage[5])},
-        reference_costs={"bvh2": float(stage[6]), "bvh8": float(stage[7])},
-        bvh8_nodes=int(nc.value), clocks=clocks.summary())
+                       "search_radius": args.radius, "sample_tris": m},
+            "cpu_baseline": {"value": round(value, 3), "unit": "Mtris/s", "cores": oracle.threads(), "kind": "port",
+                             "sample": f"first {m:,} of the workload's {n:,} triangles per step, one full CPU build "
+                                       "(bounds, Morton, radix sort, H-PLOC, BVH8)",
+                             "stage_ms": [round(x / args.steps, 1) for x in stage]},
+            "e2e": {"value": round(value, 3), "unit": "Mtris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference path has no CPU implementation; its CUDA build faulted on GB300 (Xid 31, stale-L1 "
+                    "race in BinaryBuilder.cu) and is not run again; the CPU port of its algorithm is timed"}
     print(json.dumps(line), flush=True)
 
 

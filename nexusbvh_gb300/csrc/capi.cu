@@ -146,8 +146,10 @@ nxb_status enqueue_build(const void* prims, nxb_prim_type type, uint32_t n, cons
     }
     // an even number of passes leaves the sorted keys / permutation in A
     NXB_TRY(mark(3));
-    NXB_TRY(launch_hploc(L.key_bytes, keys_a, vals_a, parent, bvh2, n, radius_of(cfg), &ctrl->cluster_count,
-                         &ctrl->error_word, s));
+    // the BVH8 work slots are not in use yet: their first 4n bytes hold the
+    // H-PLOC cluster tokens
+    NXB_TRY(launch_hploc(L.key_bytes, keys_a, vals_a, parent, bvh2, n, radius_of(cfg),
+                         reinterpret_cast<uint32_t*>(pairs), &ctrl->parent_of_last, &ctrl->error_word, s));
     NXB_TRY(mark(4));
     if (bvh8) {
         NXB_TRY(launch_bvh8_init(pairs, n, ctrl->bvh8_ctr, s));
@@ -523,7 +525,7 @@ nxb_status nxb_stage_radix_sort(uint32_t key_bytes, const void* d_keys_in, void*
     return NXB_OK;
 }
 
-size_t nxb_hploc_scratch_bytes(uint32_t n) { return align_up(4ull * n) + kAlign; }
+size_t nxb_hploc_scratch_bytes(uint32_t n) { return 2 * align_up(4ull * n) + kAlign; }
 
 nxb_status nxb_stage_hploc(uint32_t key_bytes, const void* d_sorted_keys, uint32_t* d_cluster_idx,
                            nxb_bvh2_node* d_nodes, uint32_t n, uint32_t search_radius, void* d_scratch,
@@ -535,11 +537,12 @@ nxb_status nxb_stage_hploc(uint32_t key_bytes, const void* d_sorted_keys, uint32
     if (n > kMaxPrims) return NXB_ERR_UNSUPPORTED;
     if (scratch_bytes < nxb_hploc_scratch_bytes(n)) return NXB_ERR_WORKSPACE_TOO_SMALL;
     uint32_t* parent = (uint32_t*)d_scratch;
-    uint32_t* counter = reinterpret_cast<uint32_t*>((unsigned char*)d_scratch + align_up(4ull * n));
+    uint32_t* tokens = reinterpret_cast<uint32_t*>((unsigned char*)d_scratch + align_up(4ull * n));
+    uint32_t* parent_of_last = reinterpret_cast<uint32_t*>((unsigned char*)d_scratch + 2 * align_up(4ull * n));
     NXB_TRY(launch_fill_u32(parent, kInvalid, n, stream));
-    NXB_TRY(launch_fill_u32(counter, n, 1, stream));
+    NXB_TRY(launch_fill_u32(parent_of_last, kInvalid, 1, stream));
     NXB_TRY(launch_hploc(key_bytes, d_sorted_keys, d_cluster_idx, parent, reinterpret_cast<Node2*>(d_nodes), n,
-                         search_radius, counter, d_error_word, stream));
+                         search_radius, tokens, parent_of_last, d_error_word, stream));
     return NXB_OK;
 }
 

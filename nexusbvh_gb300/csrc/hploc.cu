@@ -15,9 +15,10 @@
 //     patterns) over candidates i+1, i-1, i+2, i-2, ..., i+R, i-R.  Each
 //     pair's area is computed once and sent back to the partner with one
 //     shuffle (7 shuffles per radius step instead of 10);
-//   * the merge, node numbering by one atomicAdd per warp, and the
-//     order-preserving compaction follow MergeClustersCreateBVH2Node
-//     (:71-124).
+//   * the merge and the order-preserving compaction follow
+//     MergeClustersCreateBVH2Node (:71-124); internal nodes are numbered
+//     from the tokens of the clusters they absorb instead of from a global
+//     atomic counter (see merge_step), and the root still lands at 2n-2.
 // A window whose valid ids are not a prefix (impossible for a correct
 // climb) sets NXB_DEVERR_HPLOC_INVALID_CLUSTER instead of reading out of
 // bounds.
@@ -64,28 +65,37 @@ __device__ __forceinline__ uint32_t nearest_neighbour(uint32_t num, const Box& c
 
 struct MergeCtx {
     Node2* nodes;
-    uint32_t* counter;
-    uint32_t node_limit;
+    uint32_t* tok;             // first-leaf token of each stored cluster
+    uint32_t* parent_of_last;  // node whose child is node 2n-2 (root fix-up)
+    uint32_t n;
+    uint32_t node_limit;       // 2n-1
     uint32_t* err;
 };
 
-__device__ __forceinline__ uint32_t merge_step(const MergeCtx& m, uint32_t num, uint32_t nn, uint32_t& cid, Box& cb) {
+// One round of PLOC merging (MergeClustersCreateBVH2Node,
+// BinaryBuilder.cu:71-124).  Node numbering: every cluster carries the
+// sorted position of its first leaf (its token); merging lanes i < j keeps
+// token i, and token j is never seen again.  The n-1 merges therefore
+// absorb the tokens 1..n-1 exactly once, and node n-1+token(j) is a
+// collision-free index in [n, 2n-1) that needs no global counter (the
+// reference takes one atomicAdd on a single counter per merge round).
+__device__ __forceinline__ uint32_t merge_step(const MergeCtx& m, uint32_t num, uint32_t nn, uint32_t& cid,
+                                               uint32_t& ctok, Box& cb) {
     const uint32_t lane = lane_id();
     const uint32_t nn_of_nn = __shfl_sync(kFullMask, nn, nn & 31u);
     const bool mutual = lane < num && lane == nn_of_nn;
     const bool merge = mutual && lane < nn;
     const uint32_t mmask = __ballot_sync(kFullMask, merge);
     const uint32_t mcount = __popc(mmask);
-    uint32_t base = 0;
-    if (lane == 0 && mcount) base = atomicAdd(m.counter, mcount);
-    base = __shfl_sync(kFullMask, base, 0);
     const uint32_t ncid = __shfl_sync(kFullMask, cid, nn & 31u);
+    const uint32_t ntok = __shfl_sync(kFullMask, ctok, nn & 31u);
     const Box nb = shfl_box(cb, nn & 31u);
     if (merge) {
         grow(cb, nb);
-        const uint32_t idx = base + __popc(mmask & lanemask_lt());
-        if (idx < m.node_limit) {
+        const uint32_t idx = m.n - 1 + ntok;
+        if (idx < m.node_limit && ntok != 0) {
             store_node(m.nodes, idx, cb, cid, ncid);
+            if (cid == m.node_limit - 1 || ncid == m.node_limit - 1) atomicExch(m.parent_of_last, idx);
         } else {
             set_error(m.err, NXB_DEVERR_HPLOC_INVALID_CLUSTER);
         }
@@ -94,9 +104,58 @@ __device__ __forceinline__ uint32_t merge_step(const MergeCtx& m, uint32_t num, 
     const uint32_t vmask = __ballot_sync(kFullMask, merge || !mutual);
     const int sh = __fns(vmask, 0, lane + 1);
     cid = __shfl_sync(kFullMask, cid, (uint32_t)sh & 31u);
+    ctok = __shfl_sync(kFullMask, ctok, (uint32_t)sh & 31u);
     cb = shfl_box(cb, (uint32_t)sh & 31u);
     if (sh < 0) cid = kInvalid;
     return num - mcount;
+}
+
+// The last merge of the build (the root, two clusters left in lanes 0 and
+// 1).  The root must sit at node 2n-2, like the reference's; if the token
+// numbering put another node there, that node moves to the root's own
+// slot n-1+token(lane 1) and its parent's child index is patched.
+__device__ __forceinline__ void merge_root(const MergeCtx& m, uint32_t& cid, uint32_t& ctok, Box& cb) {
+    const uint32_t lane = lane_id();
+    const uint32_t b_cid = __shfl_sync(kFullMask, cid, 1);
+    const uint32_t b_tok = __shfl_sync(kFullMask, ctok, 1);
+    const Box b_box = shfl_box(cb, 1);
+    __syncwarp();
+    if (lane == 0) {
+        const uint32_t root = m.node_limit - 1;
+        const uint32_t natural = m.n - 1 + b_tok;
+        uint32_t a = cid, b = b_cid;
+        grow(cb, b_box);
+        if (natural != root) {
+            if (natural >= m.node_limit) {
+                set_error(m.err, NXB_DEVERR_HPLOC_INVALID_CLUSTER);
+            } else {
+                const uint4* src = reinterpret_cast<const uint4*>(m.nodes + root);
+                uint4* dst = reinterpret_cast<uint4*>(m.nodes + natural);
+                const uint4 lo = __ldcg(src), hi = __ldcg(src + 1);
+                __stcg(dst, lo);
+                __stcg(dst + 1, hi);
+                if (a == root) {
+                    a = natural;
+                } else if (b == root) {
+                    b = natural;
+                } else {
+                    const uint32_t p = __ldcg(m.parent_of_last);
+                    if (p < m.node_limit) {
+                        uint32_t* pl = reinterpret_cast<uint32_t*>(m.nodes + p) + 6;
+                        if (__ldcg(pl) == root)
+                            __stcg(pl, natural);
+                        else
+                            __stcg(pl + 1, natural);
+                    } else {
+                        set_error(m.err, NXB_DEVERR_HPLOC_INVALID_CLUSTER);
+                    }
+                }
+            }
+        }
+        store_node(m.nodes, root, cb, a, b);
+        cid = root;
+    }
+    if (lane == 1) cid = kInvalid;
 }
 
 template <int R>
@@ -108,13 +167,24 @@ __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t 
     const uint32_t mid = __shfl_sync(kFullMask, split, owner);
     const bool fin = __shfl_sync(kFullMask, final ? 1u : 0u, owner) != 0;
 
-    const uint32_t l_size = min(mid - l_start, kMergeThreshold);
-    const uint32_t r_size = min(r_end - mid, kMergeThreshold);
-    uint32_t v = kInvalid;
+    // LoadIndices (BinaryBuilder.cu:42-57) for both children at once: lanes
+    // 0-15 read the left window, lanes 16-31 the right one.  A child of at
+    // most 16 primitives was never merged, so its ids and tokens are the
+    // original ones (token = position); a larger child was stored compacted.
+    const uint32_t l_len = mid - l_start, r_len = r_end - mid;
+    const uint32_t l_size = min(l_len, kMergeThreshold);
+    const uint32_t r_size = min(r_len, kMergeThreshold);
+    uint32_t v = kInvalid, t = kInvalid;
     if (lane < 16) {
-        if (lane < l_size) v = __ldcg(cluster + l_start + lane);
+        if (lane < l_size) {
+            const uint32_t pos = l_start + lane;
+            v = __ldcg(cluster + pos);
+            t = l_len > kMergeThreshold ? __ldcg(m.tok + pos) : pos;
+        }
     } else if (lane - 16 < r_size) {
-        v = __ldcg(cluster + mid + lane - 16);
+        const uint32_t pos = mid + lane - 16;
+        v = __ldcg(cluster + pos);
+        t = r_len > kMergeThreshold ? __ldcg(m.tok + pos) : pos;
     }
     const uint32_t vb = __ballot_sync(kFullMask, v != kInvalid);
     const uint32_t num_left = __popc(vb & 0xFFFFu), num_right = __popc(vb >> 16);
@@ -123,10 +193,11 @@ __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t 
         return;
     }
     uint32_t num = num_left + num_right;
-    const uint32_t src = lane < num_left ? lane : 16u + lane - num_left;
-    uint32_t cid = __shfl_sync(kFullMask, v, src & 31u);
+    const uint32_t src = (lane < num_left ? lane : 16u + lane - num_left) & 31u;
+    uint32_t cid = __shfl_sync(kFullMask, v, src);
+    uint32_t ctok = __shfl_sync(kFullMask, t, src);
     if (lane >= num) cid = kInvalid;
-    if (__ballot_sync(kFullMask, lane < num && cid >= m.node_limit)) {
+    if (__ballot_sync(kFullMask, lane < num && (cid >= m.node_limit || ctok >= m.n))) {
         if (lane == 0) set_error(m.err, NXB_DEVERR_HPLOC_INVALID_CLUSTER);
         return;
     }
@@ -139,21 +210,30 @@ __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t 
     }
     const uint32_t threshold = fin ? 1u : kMergeThreshold;
     while (num > threshold) {
+        if (fin && num == 2) {
+            merge_root(m, cid, ctok, cb);
+            num = 1;
+            break;
+        }
         const uint32_t nn = nearest_neighbour<R>(num, cb);
-        num = merge_step(m, num, nn, cid, cb);
+        num = merge_step(m, num, nn, cid, ctok, cb);
     }
-    if (lane < num_left + num_right) __stcg(cluster + l_start + lane, cid);
+    // StoreIndices (BinaryBuilder.cu:59-69)
+    if (lane < num_left + num_right) {
+        __stcg(cluster + l_start + lane, cid);
+        __stcg(m.tok + l_start + lane, ctok);
+    }
     __threadfence();
 }
 
 template <typename K, int R>
 __global__ __launch_bounds__(kThreads) void hploc_kernel(const K* __restrict__ keys, uint32_t* cluster,
-                                                         uint32_t* parent, Node2* nodes, uint32_t n,
-                                                         uint32_t* counter, uint32_t* err) {
+                                                         uint32_t* parent, Node2* nodes, uint32_t n, uint32_t* tok,
+                                                         uint32_t* parent_of_last, uint32_t* err) {
     const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t left = idx, right = idx, split = 0;
     bool active = idx < n;
-    MergeCtx m{nodes, counter, 2 * n - 1, err};
+    MergeCtx m{nodes, tok, parent_of_last, n, 2 * n - 1, err};
     while (__ballot_sync(kFullMask, active)) {
         if (active) {
             uint32_t prev;
@@ -187,12 +267,12 @@ __global__ __launch_bounds__(kThreads) void hploc_kernel(const K* __restrict__ k
 
 template <typename K>
 cudaError_t launch_t(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, uint32_t n, uint32_t radius,
-                     uint32_t* counter, uint32_t* err, cudaStream_t s) {
+                     uint32_t* tok, uint32_t* pol, uint32_t* err, cudaStream_t s) {
     const uint32_t grid = (n + kThreads - 1) / kThreads;
     switch (radius) {
-        case 4: hploc_kernel<K, 4><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, n, counter, err); break;
-        case 16: hploc_kernel<K, 16><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, n, counter, err); break;
-        default: hploc_kernel<K, 8><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, n, counter, err); break;
+        case 4: hploc_kernel<K, 4><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, n, tok, pol, err); break;
+        case 16: hploc_kernel<K, 16><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, n, tok, pol, err); break;
+        default: hploc_kernel<K, 8><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, n, tok, pol, err); break;
     }
     return cudaGetLastError();
 }
@@ -200,10 +280,13 @@ cudaError_t launch_t(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* 
 }  // namespace
 
 cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
-                         uint32_t n, uint32_t radius, uint32_t* counter, uint32_t* err, cudaStream_t s) {
+                         uint32_t n, uint32_t radius, uint32_t* tokens, uint32_t* parent_of_last, uint32_t* err,
+                         cudaStream_t s) {
     if (key_bytes == 4)
-        return launch_t<uint32_t>((const uint32_t*)keys, cluster_idx, parent, nodes, n, radius, counter, err, s);
-    return launch_t<uint64_t>((const uint64_t*)keys, cluster_idx, parent, nodes, n, radius, counter, err, s);
+        return launch_t<uint32_t>((const uint32_t*)keys, cluster_idx, parent, nodes, n, radius, tokens,
+                                  parent_of_last, err, s);
+    return launch_t<uint64_t>((const uint64_t*)keys, cluster_idx, parent, nodes, n, radius, tokens, parent_of_last,
+                              err, s);
 }
 
 }  // namespace nxb

@@ -21,7 +21,8 @@ struct Control {
     uint32_t cluster_count; // H-PLOC node allocator
     uint32_t error_word;
     uint32_t bvh8_ctr[4];   // slot-batch claim, node counter, leaf counter, work-slot allocator
-    uint32_t pad[4];
+    uint32_t parent_of_last; // H-PLOC: the node whose child is node 2n-2 (seeded INVALID)
+    uint32_t pad[3];
     uint32_t tile_ctr[kMaxSortPasses];
     uint32_t hist[kMaxSortPasses][kRadixBins];
 };
@@ -79,8 +80,11 @@ cudaError_t launch_sort_pass(uint32_t key_bytes, const void* keys_in, void* keys
                              uint32_t* vals_out, uint32_t n, uint32_t shift, uint32_t bits, const uint32_t* hist,
                              uint32_t* lookback, uint32_t* tile_ctr, uint32_t* err, cudaStream_t s);
 // ---------------------------------------------------------------- stage 4
+// tokens: n words of scratch (no initialisation needed); parent_of_last:
+// one word that must hold INVALID on entry.
 cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
-                         uint32_t n, uint32_t radius, uint32_t* counter, uint32_t* err, cudaStream_t s);
+                         uint32_t n, uint32_t radius, uint32_t* tokens, uint32_t* parent_of_last, uint32_t* err,
+                         cudaStream_t s);
 // ---------------------------------------------------------------- stage 5
 // pairs: n uint64 slots; ctr: {claim, node, leaf, work}.  Both are
 // initialised by launch_bvh8_init (or the fused Morton seed + pair init).

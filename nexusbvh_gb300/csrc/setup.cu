@@ -163,6 +163,7 @@ __global__ __launch_bounds__(kThreads) void morton_kernel(const Node2* __restric
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (a.seed) {
             ctrl->cluster_count = n;
+            ctrl->parent_of_last = kInvalid;
             ctrl->bvh8_ctr[0] = 0;
             ctrl->bvh8_ctr[1] = 1;
             ctrl->bvh8_ctr[2] = 0;

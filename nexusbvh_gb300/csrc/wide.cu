@@ -8,7 +8,11 @@
 // bounded relaxed loads and processes whichever lanes are ready, so no
 // resident warp ever waits on a warp that has not started.  The three
 // allocation counters are bumped once per warp iteration with a warp scan
-// instead of once per node.  The decisions are the reference's:
+// instead of once per node.  Each thread keeps the children it expands in
+// a slot table in shared memory (BVH2 index, children, box), so popping a
+// child, the slot assignment and the quantisation never reload a node
+// (the reference reloads each child box up to three times).
+// The decisions are the reference's:
 //   * expansion always re-opens the highest-indexed inner child, the child
 //     with the smaller area going to the re-opened position (:284-330);
 //   * greedy slot assignment in child order, first strictly best slot
@@ -23,9 +27,11 @@
 namespace nxb {
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 128;
 constexpr float kQuantStep = 1.0f / 255.0f;  // 1/((1<<NQ)-1), NQ = 8
 constexpr uint32_t kQueueSpinLimit = 1u << 20;
+constexpr int kSlotWords = 9;  // BVH2 index, left, right, box (6 floats)
+constexpr size_t kSlotSmem = (size_t)kThreads * 8 * kSlotWords * sizeof(uint32_t);
 
 __device__ __forceinline__ uint32_t nib(uint32_t x, uint32_t i) { return (x >> (4 * i)) & 0xFu; }
 __device__ __forceinline__ uint32_t popc_below(uint32_t m, uint32_t i) { return __popc(m & ((1u << i) - 1u)); }
@@ -48,17 +54,46 @@ __device__ __forceinline__ Node2 load_node(const Node2* b2, uint32_t i) {
     return r;
 }
 
+// Per-thread table of the (up to 8) children being collected, in shared
+// memory, word-interleaved across the CTA's threads (bank-conflict free).
+struct SlotTable {
+    uint32_t* base;
+    __device__ uint32_t* at(uint32_t slot, uint32_t field) const {
+        return base + (slot * kSlotWords + field) * kThreads + threadIdx.x;
+    }
+    __device__ void put(uint32_t slot, uint32_t idx, const Node2& nd) const {
+        *at(slot, 0) = idx;
+        *at(slot, 1) = nd.left;
+        *at(slot, 2) = nd.right;
+        *at(slot, 3) = __float_as_uint(nd.b.mn.x);
+        *at(slot, 4) = __float_as_uint(nd.b.mn.y);
+        *at(slot, 5) = __float_as_uint(nd.b.mn.z);
+        *at(slot, 6) = __float_as_uint(nd.b.mx.x);
+        *at(slot, 7) = __float_as_uint(nd.b.mx.y);
+        *at(slot, 8) = __float_as_uint(nd.b.mx.z);
+    }
+    __device__ uint32_t idx(uint32_t slot) const { return *at(slot, 0); }
+    __device__ uint32_t left(uint32_t slot) const { return *at(slot, 1); }
+    __device__ uint32_t right(uint32_t slot) const { return *at(slot, 2); }
+    __device__ Box box(uint32_t slot) const {
+        Box b;
+        b.mn = make_float3(__uint_as_float(*at(slot, 3)), __uint_as_float(*at(slot, 4)), __uint_as_float(*at(slot, 5)));
+        b.mx = make_float3(__uint_as_float(*at(slot, 6)), __uint_as_float(*at(slot, 7)), __uint_as_float(*at(slot, 8)));
+        return b;
+    }
+};
+
 // GetCost (WideConverter.cu:25-30): sign pattern of slot s applied to the
 // parent-to-child centroid offset.
 __device__ __forceinline__ float slot_cost(uint32_t s, float3 o) {
     return ((s >> 2) & 1 ? -1.0f : 1.0f) * o.x + ((s >> 1) & 1 ? -1.0f : 1.0f) * o.y + (s & 1 ? -1.0f : 1.0f) * o.z;
 }
 
-__device__ __forceinline__ uint32_t greedy_assign(float3 pc, const uint32_t* child, uint32_t count,
-                                                  const Node2* b2) {
+template <typename Boxes>
+__device__ __forceinline__ uint32_t greedy_assign(float3 pc, const Boxes& boxes, uint32_t count) {
     uint32_t asg = kInvalid;
     for (uint32_t c = 0; c < count; ++c) {
-        const Box cb = load_box(b2, child[c]);
+        const Box cb = boxes.box(c);
         const float3 off = make_float3(pc.x - (cb.mx.x + cb.mn.x), pc.y - (cb.mx.y + cb.mn.y),
                                        pc.z - (cb.mx.z + cb.mn.z));
         float best = -3.402823466e+38f;
@@ -80,9 +115,9 @@ __device__ __forceinline__ uint32_t greedy_assign(float3 pc, const uint32_t* chi
     return asg;
 }
 
-__device__ __forceinline__ void write_node8(Node8* dst, const Box& bounds, const uint32_t* child, uint32_t child_base,
-                                            uint32_t prim_base, uint32_t asg, uint32_t inner, uint32_t leaf,
-                                            const Node2* b2) {
+template <typename Boxes>
+__device__ __forceinline__ void write_node8(Node8* dst, const Box& bounds, const Boxes& boxes, uint32_t child_base,
+                                            uint32_t prim_base, uint32_t asg, uint32_t inner, uint32_t leaf) {
     uint32_t w[20];
 #pragma unroll
     for (int i = 0; i < 20; ++i) w[i] = 0;
@@ -111,7 +146,7 @@ __device__ __forceinline__ void write_node8(Node8* dst, const Box& bounds, const
         }
         const uint32_t sh = 8u * (i & 3u);
         w[6 + (i >> 2)] |= meta << sh;
-        const Box cb = load_box(b2, child[a]);
+        const Box cb = boxes.box(a);
         const uint32_t qlx = (uint8_t)floorf((cb.mn.x - bounds.mn.x) * inv.x);
         const uint32_t qly = (uint8_t)floorf((cb.mn.y - bounds.mn.y) * inv.y);
         const uint32_t qlz = (uint8_t)floorf((cb.mn.z - bounds.mn.z) * inv.z);
@@ -131,6 +166,11 @@ __device__ __forceinline__ void write_node8(Node8* dst, const Box& bounds, const
     for (int k = 0; k < 5; ++k) d[k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
 }
 
+struct LeafZero {
+    const Node2* b2;
+    __device__ Box box(uint32_t) const { return load_box(b2, 0); }
+};
+
 __global__ void bvh8_init_kernel(uint64_t* pairs, uint32_t n, uint32_t* ctr) {
     const uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x;
     for (uint32_t i = i0; i < n; i += gridDim.x * blockDim.x)
@@ -146,11 +186,13 @@ __global__ void bvh8_init_kernel(uint64_t* pairs, uint32_t n, uint32_t* ctr) {
 __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict__ b2, uint32_t n, Node8* out,
                                                         uint32_t cap, uint32_t* prim_idx, uint64_t* pairs,
                                                         uint32_t* ctr, uint32_t* err) {
+    extern __shared__ uint32_t s_slots[];
+    const SlotTable tab{s_slots};
     const uint32_t lane = lane_id();
+    const uint32_t node_limit = 2 * n - 1;
     if (n == 1) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
-            uint32_t child[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            write_node8(out, load_box(b2, 0), child, 0, 0, 0xFFFFFFF0u, 0u, 1u, b2);
+            write_node8(out, load_box(b2, 0), LeafZero{b2}, 0, 0, 0xFFFFFFF0u, 0u, 1u);
             prim_idx[0] = 0;
             ctr[2] = 1;
         }
@@ -183,14 +225,14 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
             const uint32_t b2i = (uint32_t)(pr >> 32), b8i = (uint32_t)pr;
             bool internal = false;
             Node2 nd;
-            if (ready && b2i >= 2 * n - 1) {
+            if (ready && b2i >= node_limit) {
                 set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
                 active = false;
                 ready = false;
             }
             if (ready) {
                 nd = load_node(b2, b2i);
-                if (nd.left != kInvalid && (nd.left >= 2 * n - 1 || nd.right >= 2 * n - 1)) {
+                if (nd.left != kInvalid && (nd.left >= node_limit || nd.right >= node_limit)) {
                     set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
                     active = false;
                 } else if (nd.left == kInvalid) {
@@ -203,37 +245,35 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
                     internal = true;
                 }
             }
-            uint32_t child[8];
             uint32_t inner = 0, count = 0, asg = kInvalid, leaf = 0;
             if (internal) {
+                // open BVH2 nodes top-down until 8 children or no inner child
                 uint32_t l0 = nd.left, l1 = nd.right;
-                int msb = 0;
+                uint32_t msb = 0;
                 while (true) {
                     const Node2 c0 = load_node(b2, l0), c1 = load_node(b2, l1);
-                    uint32_t first = half_area(c0.b) < half_area(c1.b) ? 0u : 1u;
-#pragma unroll
-                    for (uint32_t i = 0; i < 2; ++i) {
-                        const uint32_t idx = i == 0 ? (uint32_t)msb : count;
-                        const Node2& c = first == 0 ? c0 : c1;
-                        if (c.left != kInvalid) inner |= 1u << idx;
-                        child[idx] = first == 0 ? l0 : l1;
-                        count++;
-                        first ^= 1u;
-                    }
+                    const bool first = !(half_area(c0.b) < half_area(c1.b));
+                    // the smaller-area child takes the re-opened position
+                    tab.put(msb, first ? l1 : l0, first ? c1 : c0);
+                    tab.put(count + 1, first ? l0 : l1, first ? c0 : c1);
+                    if ((first ? c1 : c0).left != kInvalid) inner |= 1u << msb;
+                    if ((first ? c0 : c1).left != kInvalid) inner |= 1u << (count + 1);
+                    count += 2;
+                    if (inner == 0 || count == 8) break;
                     msb = 31 - __clz(inner);
-                    if (msb < 0 || count == 8) break;
                     inner &= ~(1u << msb);
                     count--;
-                    const Node2 o = load_node(b2, child[msb]);
-                    l0 = o.left;
-                    l1 = o.right;
-                    if (l0 >= 2 * n - 1 || l1 >= 2 * n - 1) {  // corrupt BVH2: stop here, report
+                    l0 = tab.left(msb);
+                    l1 = tab.right(msb);
+                    if (l0 >= node_limit || l1 >= node_limit) {  // corrupt BVH2: report, stop expanding
                         set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
+                        inner |= 1u << msb;
+                        count++;
                         break;
                     }
                 }
                 const float3 pc = make_float3(nd.b.mn.x + nd.b.mx.x, nd.b.mn.y + nd.b.mx.y, nd.b.mn.z + nd.b.mx.z);
-                asg = greedy_assign(pc, child, count, b2);
+                asg = greedy_assign(pc, tab, count);
                 uint32_t ninner = 0;
 #pragma unroll
                 for (uint32_t i = 0; i < 8; ++i) {
@@ -279,17 +319,26 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
 #pragma unroll
                     for (uint32_t i = 0; i < 8; ++i) {
                         if (!((occupied >> i) & 1u)) continue;
-                        uint64_t pair = (uint64_t)child[nib(asg, i)] << 32;
+                        uint64_t pair = (uint64_t)tab.idx(nib(asg, i)) << 32;
                         pair |= (inner >> i) & 1u ? child_base + popc_below(inner, i) : prim_base + popc_below(leaf, i);
                         const uint32_t c = popc_below(occupied, i);
                         st_relaxed_u64(pairs + (c == 0 ? slot : work_base + c - 1), pair);
                     }
-                    write_node8(out + b8i, nd.b, child, child_base, prim_base, asg, inner, leaf, b2);
+                    write_node8(out + b8i, nd.b, tab, child_base, prim_base, asg, inner, leaf);
                 }
             }
             __syncwarp();
         }
     }
+}
+
+bool g_smem_configured = false;
+
+cudaError_t configure_smem() {
+    if (g_smem_configured) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(bvh8_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlotSmem);
+    if (!e) g_smem_configured = true;
+    return e;
 }
 
 }  // namespace
@@ -300,7 +349,8 @@ cudaError_t run_bvh8_stall_probe(uint32_t* err_out) {
     const uint32_t n = 2;
     unsigned char* buf = nullptr;
     const size_t bytes = 3 * sizeof(Node2) + 2 * sizeof(Node8) + 8 * n + 4 * n + 32;
-    cudaError_t e = cudaMalloc(&buf, bytes);
+    cudaError_t e = configure_smem();
+    if (!e) e = cudaMalloc(&buf, bytes);
     if (e) return e;
     Node2* b2 = (Node2*)buf;
     Node8* out = (Node8*)(buf + 3 * sizeof(Node2));
@@ -313,7 +363,7 @@ cudaError_t run_bvh8_stall_probe(uint32_t* err_out) {
     const uint32_t c[5] = {0, 1, 0, 1, 0};
     if (!e) e = cudaMemcpy(ctr, c, sizeof(c), cudaMemcpyHostToDevice);
     if (!e) {
-        bvh8_kernel<<<1, kThreads>>>(b2, n, out, 2, prim, pairs, ctr, err);
+        bvh8_kernel<<<1, kThreads, kSlotSmem>>>(b2, n, out, 2, prim, pairs, ctr, err);
         e = cudaGetLastError();
     }
     if (!e) e = cudaMemcpy(err_out, err, 4, cudaMemcpyDeviceToHost);
@@ -329,12 +379,14 @@ cudaError_t launch_bvh8_init(uint64_t* pairs, uint32_t n, uint32_t* ctr, cudaStr
 
 cudaError_t launch_bvh8(const Node2* bvh2, uint32_t n, Node8* out, uint32_t cap, uint32_t* prim_idx, uint64_t* pairs,
                         uint32_t* ctr, uint32_t* err, cudaStream_t s) {
+    cudaError_t e = configure_smem();
+    if (e) return e;
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh8_kernel, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh8_kernel, kThreads, kSlotSmem);
     if (per_sm < 1) per_sm = 1;
     uint32_t want = (n + kThreads - 1) / kThreads;
     uint32_t grid = std::max(1u, std::min(want, (uint32_t)(device_info().sms * per_sm)));
-    bvh8_kernel<<<grid, kThreads, 0, s>>>(bvh2, n, out, cap, prim_idx, pairs, ctr, err);
+    bvh8_kernel<<<grid, kThreads, kSlotSmem, s>>>(bvh2, n, out, cap, prim_idx, pairs, ctr, err);
     return cudaGetLastError();
 }
 
