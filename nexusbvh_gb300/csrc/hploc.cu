@@ -4,9 +4,12 @@
 // The decisions are the reference's, so the topology and every box are
 // identical; how they are computed on the GPU differs:
 //   * the bottom-up LBVH climb (Apetrei 2014; FindParentId/Delta,
-//     BinaryBuilder.cu:14-40) hands ranges over with acquire/release
-//     exchanges, and cross-CTA data is read through L2 (the reference reads
-//     node boxes with plain, L1-cacheable loads);
+//     BinaryBuilder.cu:14-40) hands ranges over with relaxed exchanges; a
+//     merge that reads another warp's clusters starts with an acquire
+//     fence and a merge that wrote clusters ends with a release fence, and
+//     all cross-CTA data is read through L2 (the reference reads cluster
+//     ids and node boxes with plain, L1-cacheable loads, which can return
+//     stale lines written by another SM);
 //   * LoadIndices (:42-57) loads the left and right windows of 16 cluster
 //     ids in one round trip (lanes 0-15 and 16-31) and packs them with one
 //     shuffle, instead of two dependent loads;
@@ -166,6 +169,9 @@ __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t 
     const uint32_t r_end = __shfl_sync(kFullMask, right, owner) + 1;
     const uint32_t mid = __shfl_sync(kFullMask, split, owner);
     const bool fin = __shfl_sync(kFullMask, final ? 1u : 0u, owner) != 0;
+    // acquire: the owner's relaxed exchange observed the sibling's hand-over;
+    // this fence orders the reads of the sibling's clusters after it
+    fence_acq_rel_gpu();
 
     // LoadIndices (BinaryBuilder.cu:42-57) for both children at once: lanes
     // 0-15 read the left window, lanes 16-31 the right one.  A child of at
@@ -223,7 +229,10 @@ __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t 
         __stcg(cluster + l_start + lane, cid);
         __stcg(m.tok + l_start + lane, ctok);
     }
-    __threadfence();
+    // release: every lane's node / cluster stores are ordered before the
+    // owner's next (relaxed) hand-over exchange
+    __syncwarp();
+    fence_acq_rel_gpu();
 }
 
 template <typename K, int R>
@@ -240,13 +249,13 @@ __global__ __launch_bounds__(kThreads) void hploc_kernel(const K* __restrict__ k
             const bool go_right =
                 left == 0 || (right != n - 1 && delta(keys, right, right + 1) < delta(keys, left - 1, left));
             if (go_right) {
-                prev = atom_exch_acq_rel(parent + right, left);
+                prev = atomicExch(parent + right, left);
                 if (prev != kInvalid) {
                     split = right + 1;
                     right = prev;
                 }
             } else {
-                prev = atom_exch_acq_rel(parent + left - 1, right);
+                prev = atomicExch(parent + left - 1, right);
                 if (prev != kInvalid) {
                     split = left;
                     left = prev;

@@ -20,7 +20,7 @@ struct Control {
     uint32_t scene_ord[6];  // [0..2]: ~ordered(min) (atomicMax), [3..5]: ordered(max)
     uint32_t cluster_count; // H-PLOC node allocator
     uint32_t error_word;
-    uint32_t bvh8_ctr[4];   // slot-batch claim, node counter, leaf counter, work-slot allocator
+    uint32_t bvh8_ctr[8];   // BVH8: slot claim, node counter, leaf counter, work-slot allocator, pending items
     uint32_t parent_of_last; // H-PLOC: the node whose child is node 2n-2 (seeded INVALID)
     uint32_t pad[3];
     uint32_t tile_ctr[kMaxSortPasses];

@@ -164,10 +164,6 @@ __global__ __launch_bounds__(kThreads) void morton_kernel(const Node2* __restric
         if (a.seed) {
             ctrl->cluster_count = n;
             ctrl->parent_of_last = kInvalid;
-            ctrl->bvh8_ctr[0] = 0;
-            ctrl->bvh8_ctr[1] = 1;
-            ctrl->bvh8_ctr[2] = 0;
-            ctrl->bvh8_ctr[3] = 1;
         }
         if (a.scene_out) {
             a.scene_out->bmin[0] = smin.x;

@@ -1,17 +1,21 @@
 // wide.cu - stage 5: BVH2 -> compressed 8-wide BVH (Ylitie et al. 2017).
 //
 // Replaces BuildBVH8Kernel (NexusBVH/src/Cuda/WideConverter.cu:225-414).
-// The reference launches one thread per work slot (n threads) and keeps
-// every CTA spinning in lock-step on __syncthreads_count until its slots
-// are filled.  Here a persistent grid (sized to the SM count) claims
-// batches of 32 slots in increasing order; a warp polls its batch with
-// bounded relaxed loads and processes whichever lanes are ready, so no
-// resident warp ever waits on a warp that has not started.  The three
-// allocation counters are bumped once per warp iteration with a warp scan
-// instead of once per node.  Each thread keeps the children it expands in
-// a slot table in shared memory (BVH2 index, children, box), so popping a
-// child, the slot assignment and the quantisation never reload a node
-// (the reference reloads each child box up to three times).
+// The reference launches one thread per work slot (n threads, one work
+// item per BVH8 node and one per primitive) and keeps every CTA spinning in
+// lock-step on __syncthreads_count until its slots are filled.  Here:
+//   * only internal BVH8 nodes are work items; a parent writes its leaf
+//     children's primitives into primIdx directly;
+//   * a persistent grid (occupancy x SM count) whose lanes each hold one
+//     work slot, claimed in increasing order, and poll it with bounded
+//     relaxed loads, so no resident lane ever waits on a lane that has not
+//     started;
+//   * the allocation counters are bumped once per warp iteration with a
+//     warp scan instead of once per node;
+//   * each thread keeps the children it expands in a slot table in shared
+//     memory (BVH2 index, children, box), so popping a child, the slot
+//     assignment and the quantisation never reload a node (the reference
+//     reloads each child box up to three times).
 // The decisions are the reference's:
 //   * expansion always re-opens the highest-indexed inner child, the child
 //     with the smaller area going to the re-opened position (:284-330);
@@ -176,13 +180,23 @@ __global__ void bvh8_init_kernel(uint64_t* pairs, uint32_t n, uint32_t* ctr) {
     for (uint32_t i = i0; i < n; i += gridDim.x * blockDim.x)
         pairs[i] = i == 0 ? ((uint64_t)(2 * n - 2) << 32) : ~0ull;
     if (i0 == 0) {
-        ctr[0] = 0;
-        ctr[1] = 1;
-        ctr[2] = 0;
-        ctr[3] = 1;
+        ctr[0] = 0;  // next work slot to claim
+        ctr[1] = 1;  // BVH8 nodes allocated (the root)
+        ctr[2] = 0;  // leaves allocated
+        ctr[3] = 1;  // work slots allocated (the root's)
+        ctr[4] = 1;  // work items allocated but not finished
     }
 }
 
+// Work items are the internal BVH8 nodes only: a parent writes the
+// primitive of each leaf child straight into primIdx (it holds the leaf's
+// node in its slot table), instead of queueing a work item per leaf as the
+// reference does (one per primitive, each re-reading the leaf node).  A
+// parent's first inner child continues in the parent's own slot, the others
+// get fresh slots, so a slot is always written by an item in a lower slot.
+// Each lane holds one slot at a time and claims the next one (warp-
+// aggregated) as soon as its chain ends; the kernel ends when the count of
+// allocated-but-unfinished items drops to zero.
 __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict__ b2, uint32_t n, Node8* out,
                                                         uint32_t cap, uint32_t* prim_idx, uint64_t* pairs,
                                                         uint32_t* ctr, uint32_t* err) {
@@ -195,140 +209,154 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
             write_node8(out, load_box(b2, 0), LeafZero{b2}, 0, 0, 0xFFFFFFF0u, 0u, 1u);
             prim_idx[0] = 0;
             ctr[2] = 1;
+            ctr[4] = 0;
         }
         return;
     }
+    uint32_t slot = kInvalid;
+    bool retired = false;
+    uint32_t idle = 0;
     for (;;) {
-        uint32_t batch = 0;
-        if (lane == 0) batch = atomicAdd(ctr, 32u);
-        batch = __shfl_sync(kFullMask, batch, 0);
-        if (batch >= n) return;
-        const uint32_t slot = batch + lane;
-        bool active = slot < n;
-        uint32_t idle = 0;
-        while (__any_sync(kFullMask, active)) {
-            uint64_t pr = 0;
-            bool ready = false;
-            if (active) {
-                pr = ld_relaxed_u64(pairs + slot);
-                ready = (uint32_t)(pr >> 32) != kInvalid;
-            }
-            if (!__any_sync(kFullMask, ready)) {
-                if (++idle > kQueueSpinLimit) {
-                    if (lane == 0) set_error(err, NXB_DEVERR_BVH8_QUEUE_TIMEOUT);
-                    return;
+        // lanes without a slot claim the next ones, in increasing order
+        const bool want = !retired && slot == kInvalid;
+        const uint32_t wmask = __ballot_sync(kFullMask, want);
+        if (wmask) {
+            const uint32_t leader = __ffs(wmask) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(ctr, (uint32_t)__popc(wmask));
+            base = __shfl_sync(kFullMask, base, leader);
+            if (want) {
+                slot = base + __popc(wmask & lanemask_lt());
+                if (slot >= n) {
+                    slot = kInvalid;
+                    retired = true;
                 }
-                __nanosleep(100);
-                continue;
             }
-            idle = 0;
-            const uint32_t b2i = (uint32_t)(pr >> 32), b8i = (uint32_t)pr;
-            bool internal = false;
-            Node2 nd;
-            if (ready && b2i >= node_limit) {
+        }
+        if (__all_sync(kFullMask, retired)) return;
+        uint64_t pr = 0;
+        bool ready = false;
+        if (slot != kInvalid) {
+            pr = ld_relaxed_u64(pairs + slot);
+            ready = (uint32_t)(pr >> 32) != kInvalid;
+        }
+        if (!__any_sync(kFullMask, ready)) {
+            // nothing ready: finished when no allocated item is outstanding
+            if (ld_relaxed_u32(ctr + 4) == 0) return;
+            if (++idle > kQueueSpinLimit) {
+                if (lane == 0) set_error(err, NXB_DEVERR_BVH8_QUEUE_TIMEOUT);
+                return;
+            }
+            __nanosleep(64);
+            continue;
+        }
+        idle = 0;
+        const uint32_t b2i = (uint32_t)(pr >> 32), b8i = (uint32_t)pr;
+        bool internal = false;
+        Node2 nd;
+        if (ready) {
+            if (b2i >= node_limit || b8i >= cap) {
                 set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
-                active = false;
-                ready = false;
-            }
-            if (ready) {
+            } else {
                 nd = load_node(b2, b2i);
-                if (nd.left != kInvalid && (nd.left >= node_limit || nd.right >= node_limit)) {
+                if (nd.left >= node_limit || nd.right >= node_limit)
                     set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
-                    active = false;
-                } else if (nd.left == kInvalid) {
-                    if (b8i < n)
-                        prim_idx[b8i] = nd.right;
-                    else
-                        set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
-                    active = false;
-                } else {
+                else
                     internal = true;
+            }
+            if (!internal) slot = kInvalid;  // reported; the item counts as finished
+        }
+        uint32_t inner = 0, count = 0, asg = kInvalid, leaf = 0;
+        if (internal) {
+            // open BVH2 nodes top-down until 8 children or no inner child
+            uint32_t l0 = nd.left, l1 = nd.right;
+            uint32_t msb = 0;
+            while (true) {
+                const Node2 c0 = load_node(b2, l0), c1 = load_node(b2, l1);
+                const bool first = !(half_area(c0.b) < half_area(c1.b));
+                // the smaller-area child takes the re-opened position
+                tab.put(msb, first ? l1 : l0, first ? c1 : c0);
+                tab.put(count + 1, first ? l0 : l1, first ? c0 : c1);
+                if ((first ? c1 : c0).left != kInvalid) inner |= 1u << msb;
+                if ((first ? c0 : c1).left != kInvalid) inner |= 1u << (count + 1);
+                count += 2;
+                if (inner == 0 || count == 8) break;
+                msb = 31 - __clz(inner);
+                inner &= ~(1u << msb);
+                count--;
+                l0 = tab.left(msb);
+                l1 = tab.right(msb);
+                if (l0 >= node_limit || l1 >= node_limit) {  // corrupt BVH2: report, stop expanding
+                    set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
+                    inner |= 1u << msb;
+                    count++;
+                    break;
                 }
             }
-            uint32_t inner = 0, count = 0, asg = kInvalid, leaf = 0;
-            if (internal) {
-                // open BVH2 nodes top-down until 8 children or no inner child
-                uint32_t l0 = nd.left, l1 = nd.right;
-                uint32_t msb = 0;
-                while (true) {
-                    const Node2 c0 = load_node(b2, l0), c1 = load_node(b2, l1);
-                    const bool first = !(half_area(c0.b) < half_area(c1.b));
-                    // the smaller-area child takes the re-opened position
-                    tab.put(msb, first ? l1 : l0, first ? c1 : c0);
-                    tab.put(count + 1, first ? l0 : l1, first ? c0 : c1);
-                    if ((first ? c1 : c0).left != kInvalid) inner |= 1u << msb;
-                    if ((first ? c0 : c1).left != kInvalid) inner |= 1u << (count + 1);
-                    count += 2;
-                    if (inner == 0 || count == 8) break;
-                    msb = 31 - __clz(inner);
-                    inner &= ~(1u << msb);
-                    count--;
-                    l0 = tab.left(msb);
-                    l1 = tab.right(msb);
-                    if (l0 >= node_limit || l1 >= node_limit) {  // corrupt BVH2: report, stop expanding
-                        set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
-                        inner |= 1u << msb;
-                        count++;
-                        break;
-                    }
-                }
-                const float3 pc = make_float3(nd.b.mn.x + nd.b.mx.x, nd.b.mn.y + nd.b.mx.y, nd.b.mn.z + nd.b.mx.z);
-                asg = greedy_assign(pc, tab, count);
-                uint32_t ninner = 0;
+            const float3 pc = make_float3(nd.b.mn.x + nd.b.mx.x, nd.b.mn.y + nd.b.mx.y, nd.b.mn.z + nd.b.mx.z);
+            asg = greedy_assign(pc, tab, count);
+            uint32_t ninner = 0;
+#pragma unroll
+            for (uint32_t i = 0; i < 8; ++i) {
+                const uint32_t a = nib(asg, i);
+                if (a == 0xFu) continue;
+                const uint32_t bit = (inner >> a) & 1u;
+                ninner |= bit << i;
+                leaf |= (bit ^ 1u) << i;
+            }
+            inner = ninner;
+        }
+        // warp-aggregated allocation of inner nodes, leaves and work slots
+        const uint32_t ic = internal ? (uint32_t)__popc(inner) : 0u;
+        const uint32_t lc = internal ? count - ic : 0u;
+        const uint32_t wc = ic > 0 ? ic - 1u : 0u;
+        const uint32_t packed = ic | (lc << 10) | (wc << 20);
+        uint32_t incl = packed;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        const uint32_t done = __popc(__ballot_sync(kFullMask, ready));
+        uint32_t bases[3] = {0, 0, 0};
+        if (lane == 31) {
+            const uint32_t tn = incl & 0x3FFu, tl = (incl >> 10) & 0x3FFu, tw = incl >> 20;
+            if (tn) bases[0] = atomicAdd(ctr + 1, tn);
+            if (tl) bases[1] = atomicAdd(ctr + 2, tl);
+            if (tw) bases[2] = atomicAdd(ctr + 3, tw);
+        }
+        const uint32_t nb = __shfl_sync(kFullMask, bases[0], 31);
+        const uint32_t lb = __shfl_sync(kFullMask, bases[1], 31);
+        const uint32_t wb = __shfl_sync(kFullMask, bases[2], 31);
+        if (internal) {
+            const uint32_t excl = incl - packed;
+            const uint32_t child_base = nb + (excl & 0x3FFu);
+            const uint32_t prim_base = lc ? lb + ((excl >> 10) & 0x3FFu) : 0u;
+            const uint32_t work_base = wb + (excl >> 20);
+            if (child_base + ic > cap || work_base + wc > n || prim_base + lc > n) {
+                set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
+                slot = kInvalid;
+            } else {
 #pragma unroll
                 for (uint32_t i = 0; i < 8; ++i) {
                     const uint32_t a = nib(asg, i);
-                    if (a == 0xFu) continue;
-                    const uint32_t bit = (inner >> a) & 1u;
-                    ninner |= bit << i;
-                    leaf |= (bit ^ 1u) << i;
-                }
-                inner = ninner;
-            }
-            // warp-aggregated allocation of inner nodes, leaves and work slots
-            const uint32_t ic = internal ? (uint32_t)__popc(inner) : 0u;
-            const uint32_t lc = internal ? count - ic : 0u;
-            const uint32_t wc = internal ? count - 1u : 0u;
-            const uint32_t packed = ic | (lc << 10) | (wc << 20);
-            uint32_t incl = packed;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
-                if (lane >= (uint32_t)o) incl += y;
-            }
-            uint32_t bases[3] = {0, 0, 0};
-            if (lane == 31) {
-                const uint32_t tn = incl & 0x3FFu, tl = (incl >> 10) & 0x3FFu, tw = incl >> 20;
-                if (tn) bases[0] = atomicAdd(ctr + 1, tn);
-                if (tl) bases[1] = atomicAdd(ctr + 2, tl);
-                if (tw) bases[2] = atomicAdd(ctr + 3, tw);
-            }
-            const uint32_t nb = __shfl_sync(kFullMask, bases[0], 31);
-            const uint32_t lb = __shfl_sync(kFullMask, bases[1], 31);
-            const uint32_t wb = __shfl_sync(kFullMask, bases[2], 31);
-            if (internal) {
-                const uint32_t excl = incl - packed;
-                const uint32_t child_base = nb + (excl & 0x3FFu);
-                const uint32_t prim_base = lc ? lb + ((excl >> 10) & 0x3FFu) : 0u;
-                const uint32_t work_base = wb + (excl >> 20);
-                if (child_base + ic > cap || work_base + wc > n || b8i >= cap) {
-                    set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
-                    active = false;
-                } else {
-                    const uint32_t occupied = inner | leaf;
-#pragma unroll
-                    for (uint32_t i = 0; i < 8; ++i) {
-                        if (!((occupied >> i) & 1u)) continue;
-                        uint64_t pair = (uint64_t)tab.idx(nib(asg, i)) << 32;
-                        pair |= (inner >> i) & 1u ? child_base + popc_below(inner, i) : prim_base + popc_below(leaf, i);
-                        const uint32_t c = popc_below(occupied, i);
-                        st_relaxed_u64(pairs + (c == 0 ? slot : work_base + c - 1), pair);
+                    if ((inner >> i) & 1u) {
+                        const uint32_t k = popc_below(inner, i);
+                        const uint64_t pair = ((uint64_t)tab.idx(a) << 32) | (child_base + k);
+                        st_relaxed_u64(pairs + (k == 0 ? slot : work_base + k - 1), pair);
+                    } else if ((leaf >> i) & 1u) {
+                        prim_idx[prim_base + popc_below(leaf, i)] = tab.right(a);
                     }
-                    write_node8(out + b8i, nd.b, tab, child_base, prim_base, asg, inner, leaf);
                 }
+                write_node8(out + b8i, nd.b, tab, child_base, prim_base, asg, inner, leaf);
+                if (ic == 0) slot = kInvalid;
             }
-            __syncwarp();
         }
+        // pending += items allocated - items finished (one atomic, so it can
+        // only reach zero when no item is in flight)
+        __syncwarp();
+        const uint32_t new_items = __shfl_sync(kFullMask, incl >> 20, 31) + __popc(__ballot_sync(kFullMask, ic > 0));
+        if (lane == 0 && new_items != done) atomicAdd(ctr + 4, new_items - done);
     }
 }
 
@@ -348,7 +376,7 @@ cudaError_t configure_smem() {
 cudaError_t run_bvh8_stall_probe(uint32_t* err_out) {
     const uint32_t n = 2;
     unsigned char* buf = nullptr;
-    const size_t bytes = 3 * sizeof(Node2) + 2 * sizeof(Node8) + 8 * n + 4 * n + 32;
+    const size_t bytes = 3 * sizeof(Node2) + 2 * sizeof(Node8) + 8 * n + 4 * n + 64;
     cudaError_t e = configure_smem();
     if (!e) e = cudaMalloc(&buf, bytes);
     if (e) return e;
@@ -357,10 +385,10 @@ cudaError_t run_bvh8_stall_probe(uint32_t* err_out) {
     uint64_t* pairs = (uint64_t*)(buf + 3 * sizeof(Node2) + 2 * sizeof(Node8));
     uint32_t* prim = (uint32_t*)(pairs + n);
     uint32_t* ctr = prim + n;
-    uint32_t* err = ctr + 4;
+    uint32_t* err = ctr + 5;
     e = cudaMemset(buf, 0, bytes);
     if (!e) e = cudaMemset(pairs, 0xFF, 8 * n);
-    const uint32_t c[5] = {0, 1, 0, 1, 0};
+    const uint32_t c[6] = {0, 1, 0, 1, 1, 0};  // pending = 1: the never-seeded root
     if (!e) e = cudaMemcpy(ctr, c, sizeof(c), cudaMemcpyHostToDevice);
     if (!e) {
         bvh8_kernel<<<1, kThreads, kSlotSmem>>>(b2, n, out, 2, prim, pairs, ctr, err);
