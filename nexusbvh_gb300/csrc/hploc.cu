@@ -25,6 +25,8 @@
 // A window whose valid ids are not a prefix (impossible for a correct
 // climb) sets NXB_DEVERR_HPLOC_INVALID_CLUSTER instead of reading out of
 // bounds.
+#include <algorithm>
+
 #include "pipeline.h"
 
 namespace nxb {
@@ -169,9 +171,6 @@ __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t 
     const uint32_t r_end = __shfl_sync(kFullMask, right, owner) + 1;
     const uint32_t mid = __shfl_sync(kFullMask, split, owner);
     const bool fin = __shfl_sync(kFullMask, final ? 1u : 0u, owner) != 0;
-    // acquire: the owner's relaxed exchange observed the sibling's hand-over;
-    // this fence orders the reads of the sibling's clusters after it
-    fence_acq_rel_gpu();
 
     // LoadIndices (BinaryBuilder.cu:42-57) for both children at once: lanes
     // 0-15 read the left window, lanes 16-31 the right one.  A child of at
@@ -229,73 +228,163 @@ __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t 
         __stcg(cluster + l_start + lane, cid);
         __stcg(m.tok + l_start + lane, ctok);
     }
-    // release: every lane's node / cluster stores are ordered before the
-    // owner's next (relaxed) hand-over exchange
-    __syncwarp();
-    fence_acq_rel_gpu();
 }
 
+// The climb as a work queue.  A task is one step of the bottom-up climb
+// from an LBVH node whose clusters are final: find the parent side
+// (FindParentId), exchange on the parent's hand-over slot, and, when this
+// is the second child to arrive, merge the parent (PlocMerge, if it spans
+// more than 16 primitives or is the root) and push the parent as a new
+// task.  Slots 0..n-1 are the leaves; each internal node is pushed exactly
+// once, so slots n..2n-2 fill up in push order and the queue holds exactly
+// 2n-1 tasks.  The reference runs one thread per leaf, and a warp stays
+// resident for as long as any of its lanes still climbs (most stop after a
+// step or two); here every warp pass works on 32 tasks.  Lanes claim slots
+// in increasing order, and a slot is only ever written by a lane working on
+// a lower slot, so a waiting lane always waits on a lane that is running.
+// Memory order: pushed tasks carry merged clusters, so a lane fences
+// (acquire) after reading pushed tasks, before its hand-over exchange
+// (release); merges fence (acquire) after the exchanges and (release)
+// before the pushes.
 template <typename K, int R>
 __global__ __launch_bounds__(kThreads) void hploc_kernel(const K* __restrict__ keys, uint32_t* cluster,
                                                          uint32_t* parent, Node2* nodes, uint32_t n, uint32_t* tok,
-                                                         uint32_t* parent_of_last, uint32_t* err) {
-    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t left = idx, right = idx, split = 0;
-    bool active = idx < n;
+                                                         uint32_t* parent_of_last, uint64_t* tasks, uint32_t* queue,
+                                                         uint32_t* err) {
+    const uint32_t lane = lane_id();
+    const uint32_t total = 2 * n - 1;
     MergeCtx m{nodes, tok, parent_of_last, n, 2 * n - 1, err};
-    while (__ballot_sync(kFullMask, active)) {
-        if (active) {
-            uint32_t prev;
-            const bool go_right =
-                left == 0 || (right != n - 1 && delta(keys, right, right + 1) < delta(keys, left - 1, left));
-            if (go_right) {
-                prev = atomicExch(parent + right, left);
-                if (prev != kInvalid) {
-                    split = right + 1;
-                    right = prev;
-                }
-            } else {
-                prev = atomicExch(parent + left - 1, right);
-                if (prev != kInvalid) {
-                    split = left;
-                    left = prev;
+    uint32_t slot = kInvalid;
+    bool retired = false;
+    uint32_t idle = 0;
+    for (;;) {
+        const bool want = !retired && slot == kInvalid;
+        const uint32_t wmask = __ballot_sync(kFullMask, want);
+        if (wmask) {
+            const uint32_t leader = __ffs(wmask) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(queue, (uint32_t)__popc(wmask));
+            base = __shfl_sync(kFullMask, base, leader);
+            if (want) {
+                slot = base + __popc(wmask & lanemask_lt());
+                if (slot >= total) {
+                    slot = kInvalid;
+                    retired = true;
                 }
             }
-            if (prev == kInvalid) active = false;
+        }
+        if (__all_sync(kFullMask, retired)) return;
+        uint32_t left = 0, right = 0;
+        bool ready = false;
+        if (slot < n) {
+            left = right = slot;
+            ready = true;
+        } else if (slot != kInvalid) {
+            const uint64_t t = ld_relaxed_u64(tasks + (slot - n));
+            if (t != ~0ull) {
+                left = (uint32_t)t;
+                right = (uint32_t)(t >> 32);
+                ready = true;
+            }
+        }
+        if (!__any_sync(kFullMask, ready)) {
+            if (++idle > kSpinLimit) {
+                if (lane == 0) set_error(err, NXB_DEVERR_HPLOC_QUEUE_TIMEOUT);
+                return;
+            }
+            __nanosleep(64);
+            continue;
+        }
+        idle = 0;
+        if (__any_sync(kFullMask, ready && slot >= n)) fence_acq_rel_gpu();
+        bool second = false;
+        uint32_t split = 0;
+        if (ready) {
+            slot = kInvalid;
+            if (left > right || right >= n) {
+                set_error(err, NXB_DEVERR_HPLOC_INVALID_CLUSTER);
+            } else {
+                uint32_t prev;
+                const bool go_right =
+                    left == 0 || (right != n - 1 && delta(keys, right, right + 1) < delta(keys, left - 1, left));
+                if (go_right) {
+                    prev = atomicExch(parent + right, left);
+                    if (prev != kInvalid) {
+                        split = right + 1;
+                        right = prev;
+                    }
+                } else {
+                    prev = atomicExch(parent + left - 1, right);
+                    if (prev != kInvalid) {
+                        split = left;
+                        left = prev;
+                    }
+                }
+                second = prev != kInvalid;
+            }
         }
         const uint32_t size = right - left + 1;
-        const bool final = active && size == n;
-        uint32_t todo = __ballot_sync(kFullMask, active && (size > kMergeThreshold || final));
-        while (todo) {
-            const uint32_t owner = __ffs(todo) - 1;
-            ploc_merge<R>(owner, left, right, split, final, cluster, m);
-            todo &= todo - 1;
+        const bool final = second && size == n;
+        uint32_t todo = __ballot_sync(kFullMask, second && (size > kMergeThreshold || final));
+        if (todo) {
+            fence_acq_rel_gpu();  // acquire: the siblings' clusters
+            while (todo) {
+                const uint32_t owner = __ffs(todo) - 1;
+                ploc_merge<R>(owner, left, right, split, final, cluster, m);
+                todo &= todo - 1;
+            }
+            __syncwarp();
+            fence_acq_rel_gpu();  // release: clusters and nodes before the pushes
+        }
+        const uint32_t pmask = __ballot_sync(kFullMask, second);
+        if (pmask) {
+            const uint32_t leader = __ffs(pmask) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(queue + 1, (uint32_t)__popc(pmask));
+            base = __shfl_sync(kFullMask, base, leader);
+            if (second) {
+                const uint32_t at = base + __popc(pmask & lanemask_lt());
+                if (at < n - 1)
+                    st_relaxed_u64(tasks + at, ((uint64_t)right << 32) | left);
+                else
+                    set_error(err, NXB_DEVERR_HPLOC_INVALID_CLUSTER);
+            }
         }
     }
+}
+
+template <typename K, int R>
+cudaError_t launch_r(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, uint32_t n, uint32_t* tok,
+                     uint32_t* pol, uint64_t* tasks, uint32_t* queue, uint32_t* err, cudaStream_t s) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hploc_kernel<K, R>, kThreads, 0);
+    if (per_sm < 1) per_sm = 1;
+    const uint32_t want = (2 * n - 1 + kThreads - 1) / kThreads;
+    const uint32_t grid = std::max(1u, std::min(want, (uint32_t)(device_info().sms * per_sm)));
+    hploc_kernel<K, R><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, n, tok, pol, tasks, queue, err);
+    return cudaGetLastError();
 }
 
 template <typename K>
 cudaError_t launch_t(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, uint32_t n, uint32_t radius,
-                     uint32_t* tok, uint32_t* pol, uint32_t* err, cudaStream_t s) {
-    const uint32_t grid = (n + kThreads - 1) / kThreads;
+                     uint32_t* tok, uint32_t* pol, uint64_t* tasks, uint32_t* queue, uint32_t* err, cudaStream_t s) {
     switch (radius) {
-        case 4: hploc_kernel<K, 4><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, n, tok, pol, err); break;
-        case 16: hploc_kernel<K, 16><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, n, tok, pol, err); break;
-        default: hploc_kernel<K, 8><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, n, tok, pol, err); break;
+        case 4: return launch_r<K, 4>(keys, cluster, parent, nodes, n, tok, pol, tasks, queue, err, s);
+        case 16: return launch_r<K, 16>(keys, cluster, parent, nodes, n, tok, pol, tasks, queue, err, s);
+        default: return launch_r<K, 8>(keys, cluster, parent, nodes, n, tok, pol, tasks, queue, err, s);
     }
-    return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
-                         uint32_t n, uint32_t radius, uint32_t* tokens, uint32_t* parent_of_last, uint32_t* err,
-                         cudaStream_t s) {
+                         uint32_t n, uint32_t radius, uint32_t* tokens, uint32_t* parent_of_last, uint64_t* tasks,
+                         uint32_t* queue, uint32_t* err, cudaStream_t s) {
     if (key_bytes == 4)
         return launch_t<uint32_t>((const uint32_t*)keys, cluster_idx, parent, nodes, n, radius, tokens,
-                                  parent_of_last, err, s);
+                                  parent_of_last, tasks, queue, err, s);
     return launch_t<uint64_t>((const uint64_t*)keys, cluster_idx, parent, nodes, n, radius, tokens, parent_of_last,
-                              err, s);
+                              tasks, queue, err, s);
 }
 
 }  // namespace nxb

@@ -142,6 +142,8 @@ struct MortonArgs {
     uint32_t* parent;
     uint4* zero_ptr;
     size_t zero_vec4;
+    uint4* ones_ptr;
+    size_t ones_vec4;
     nxb_aabb* scene_out;
     int seed;
 };
@@ -202,6 +204,8 @@ __global__ __launch_bounds__(kThreads) void morton_kernel(const Node2* __restric
     }
     for (size_t w = (size_t)blockIdx.x * kThreads + threadIdx.x; w < a.zero_vec4; w += stride)
         a.zero_ptr[w] = make_uint4(0, 0, 0, 0);
+    for (size_t w = (size_t)blockIdx.x * kThreads + threadIdx.x; w < a.ones_vec4; w += stride)
+        a.ones_ptr[w] = make_uint4(kInvalid, kInvalid, kInvalid, kInvalid);
     if (HIST) {
         __syncthreads();
         for (int i = threadIdx.x; i < a.pd.passes * kRadixBins; i += kThreads)
@@ -277,6 +281,8 @@ cudaError_t launch_morton(const Node2* nodes, uint32_t n, Control* ctrl, int key
     a.parent = f.parent;
     a.zero_ptr = reinterpret_cast<uint4*>(f.zero_ptr);
     a.zero_vec4 = f.zero_words / 4;
+    a.ones_ptr = reinterpret_cast<uint4*>(f.ones_ptr);
+    a.ones_vec4 = f.ones_words / 4;
     a.scene_out = f.scene_out;
     a.seed = f.seed_counters ? 1 : 0;
     uint32_t grid = grid_for(n, 8);
