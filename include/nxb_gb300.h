@@ -190,7 +190,6 @@ typedef struct nxb_build_result {
 #define NXB_DEVERR_BVH8_QUEUE_TIMEOUT    0x2u
 #define NXB_DEVERR_HPLOC_INVALID_CLUSTER 0x4u
 #define NXB_DEVERR_BVH8_OVERFLOW         0x8u
-#define NXB_DEVERR_HPLOC_QUEUE_TIMEOUT   0x10u
 
 /* Enqueues the whole BVH2 (+ optional BVH8) build on `stream` with no
  * allocation, no host synchronisation and no host<->device copy, so it can

@@ -132,8 +132,6 @@ nxb_status enqueue_build(const void* prims, nxb_prim_type type, uint32_t n, cons
     f.parent = parent;
     f.zero_ptr = lookback;
     f.zero_words = align_up(4ull * L.tiles_words) / 4;
-    f.ones_ptr = reinterpret_cast<uint32_t*>(pairs);  // the H-PLOC task queue starts empty
-    f.ones_words = align_up(8ull * n) / 4;
     f.scene_out = nullptr;
     f.seed_counters = true;
     NXB_TRY(launch_morton(bvh2, n, ctrl, (int)key_bits, keys_a, f, s));
@@ -148,10 +146,9 @@ nxb_status enqueue_build(const void* prims, nxb_prim_type type, uint32_t n, cons
     }
     // an even number of passes leaves the sorted keys / permutation in A
     NXB_TRY(mark(3));
-    // the sort's second value buffer holds the H-PLOC cluster tokens and the
-    // BVH8 work slots (not in use yet) hold the H-PLOC task queue
+    // the sort's second value buffer holds the H-PLOC cluster tokens
     NXB_TRY(launch_hploc(L.key_bytes, keys_a, vals_a, parent, bvh2, n, radius_of(cfg), vals_b,
-                         &ctrl->parent_of_last, pairs, ctrl->hploc_queue, &ctrl->error_word, s));
+                         &ctrl->parent_of_last, &ctrl->hploc_leaf_ctr, &ctrl->error_word, s));
     NXB_TRY(mark(4));
     if (bvh8) {
         NXB_TRY(launch_bvh8_init(pairs, n, ctrl->bvh8_ctr, s));
@@ -165,7 +162,7 @@ nxb_status enqueue_build(const void* prims, nxb_prim_type type, uint32_t n, cons
 
 nxb_status status_from_error_word(uint32_t w) {
     if (w == 0) return NXB_OK;
-    if (w & (NXB_DEVERR_SORT_LOOKBACK_TIMEOUT | NXB_DEVERR_BVH8_QUEUE_TIMEOUT | NXB_DEVERR_HPLOC_QUEUE_TIMEOUT))
+    if (w & (NXB_DEVERR_SORT_LOOKBACK_TIMEOUT | NXB_DEVERR_BVH8_QUEUE_TIMEOUT))
         return NXB_ERR_DEVICE_TIMEOUT;
     return NXB_ERR_DEVICE_INVARIANT;
 }
@@ -528,8 +525,8 @@ nxb_status nxb_stage_radix_sort(uint32_t key_bytes, const void* d_keys_in, void*
     return NXB_OK;
 }
 
-// parent slots (4n) | cluster tokens (4n) | task queue (8n) | 3 counters
-size_t nxb_hploc_scratch_bytes(uint32_t n) { return 2 * align_up(4ull * n) + align_up(8ull * n) + kAlign; }
+// parent slots (4n) | cluster tokens (4n) | 2 counters
+size_t nxb_hploc_scratch_bytes(uint32_t n) { return 2 * align_up(4ull * n) + kAlign; }
 
 nxb_status nxb_stage_hploc(uint32_t key_bytes, const void* d_sorted_keys, uint32_t* d_cluster_idx,
                            nxb_bvh2_node* d_nodes, uint32_t n, uint32_t search_radius, void* d_scratch,
@@ -543,14 +540,12 @@ nxb_status nxb_stage_hploc(uint32_t key_bytes, const void* d_sorted_keys, uint32
     unsigned char* base = (unsigned char*)d_scratch;
     uint32_t* parent = (uint32_t*)base;
     uint32_t* tokens = reinterpret_cast<uint32_t*>(base + align_up(4ull * n));
-    uint64_t* tasks = reinterpret_cast<uint64_t*>(base + 2 * align_up(4ull * n));
-    uint32_t* words = reinterpret_cast<uint32_t*>(base + 2 * align_up(4ull * n) + align_up(8ull * n));
+    uint32_t* words = reinterpret_cast<uint32_t*>(base + 2 * align_up(4ull * n));
     NXB_TRY(launch_fill_u32(parent, kInvalid, n, stream));
-    NXB_TRY(launch_fill_u32(reinterpret_cast<uint32_t*>(tasks), kInvalid, 2ull * n, stream));
     NXB_TRY(launch_fill_u32(words, kInvalid, 1, stream));  // parent_of_last
-    NXB_TRY(launch_fill_u32(words + 1, 0, 2, stream));      // queue counters
+    NXB_TRY(launch_fill_u32(words + 1, 0, 1, stream));      // leaf counter
     NXB_TRY(launch_hploc(key_bytes, d_sorted_keys, d_cluster_idx, parent, reinterpret_cast<Node2*>(d_nodes), n,
-                         search_radius, tokens, words, tasks, words + 1, d_error_word, stream));
+                         search_radius, tokens, words, words + 1, d_error_word, stream));
     return NXB_OK;
 }
 

@@ -4,12 +4,13 @@
 // The decisions are the reference's, so the topology and every box are
 // identical; how they are computed on the GPU differs:
 //   * the bottom-up LBVH climb (Apetrei 2014; FindParentId/Delta,
-//     BinaryBuilder.cu:14-40) hands ranges over with relaxed exchanges; a
-//     merge that reads another warp's clusters starts with an acquire
-//     fence and a merge that wrote clusters ends with a release fence, and
-//     all cross-CTA data is read through L2 (the reference reads cluster
-//     ids and node boxes with plain, L1-cacheable loads, which can return
-//     stale lines written by another SM);
+//     BinaryBuilder.cu:14-40) runs on a persistent grid whose lanes take a
+//     new leaf as soon as their climb stops (see hploc_kernel); ranges are
+//     handed over with relaxed exchanges, a pass that merges is bracketed by
+//     acquire/release fences, and all cross-CTA data is read through L2
+//     (the reference reads cluster ids and node boxes with plain,
+//     L1-cacheable loads, which can return stale lines written by another
+//     SM);
 //   * LoadIndices (:42-57) loads the left and right windows of 16 cluster
 //     ids in one round trip (lanes 0-15 and 16-31) and packs them with one
 //     shuffle, instead of two dependent loads;
@@ -230,98 +231,76 @@ __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t 
     }
 }
 
-// The climb as a work queue.  A task is one step of the bottom-up climb
-// from an LBVH node whose clusters are final: find the parent side
-// (FindParentId), exchange on the parent's hand-over slot, and, when this
-// is the second child to arrive, merge the parent (PlocMerge, if it spans
-// more than 16 primitives or is the root) and push the parent as a new
-// task.  Slots 0..n-1 are the leaves; each internal node is pushed exactly
-// once, so slots n..2n-2 fill up in push order and the queue holds exactly
-// 2n-1 tasks.  The reference runs one thread per leaf, and a warp stays
-// resident for as long as any of its lanes still climbs (most stop after a
-// step or two); here every warp pass works on 32 tasks.  Lanes claim slots
-// in increasing order, and a slot is only ever written by a lane working on
-// a lower slot, so a waiting lane always waits on a lane that is running.
-// Memory order: pushed tasks carry merged clusters, so a lane fences
-// (acquire) after reading pushed tasks, before its hand-over exchange
-// (release); merges fence (acquire) after the exchanges and (release)
-// before the pushes.
+// The climb with lane refill.  Each lane climbs from a leaf as in the
+// reference (FindParentId, exchange on the parent's hand-over slot, merge
+// and continue when second to arrive), but a lane that stops takes the next
+// unclaimed leaf from its warp's chunk (chunks of kLeafChunk leaves are
+// claimed with one atomicAdd), instead of idling until every lane of its
+// warp has finished: the reference runs one thread per leaf, and a warp
+// stays resident for as long as any of its lanes still climbs (most stop
+// after a step or two).  Nothing waits on another warp.
+// Memory order: the hand-over exchanges are relaxed; a pass that merges
+// fences (acquire) after its exchanges, before reading the siblings'
+// clusters, and (release) after its merges, before the next exchanges.
+constexpr uint32_t kLeafChunk = 64;
+
 template <typename K, int R>
 __global__ __launch_bounds__(kThreads) void hploc_kernel(const K* __restrict__ keys, uint32_t* cluster,
                                                          uint32_t* parent, Node2* nodes, uint32_t n, uint32_t* tok,
-                                                         uint32_t* parent_of_last, uint64_t* tasks, uint32_t* queue,
+                                                         uint32_t* parent_of_last, uint32_t* leaf_ctr,
                                                          uint32_t* err) {
     const uint32_t lane = lane_id();
-    const uint32_t total = 2 * n - 1;
     MergeCtx m{nodes, tok, parent_of_last, n, 2 * n - 1, err};
-    uint32_t slot = kInvalid;
-    bool retired = false;
-    uint32_t idle = 0;
+    uint32_t left = 0, right = 0, split = 0;
+    bool active = false;
+    uint32_t chunk_next = 0, chunk_end = 0;  // warp-uniform
+    bool exhausted = false;                  // warp-uniform
     for (;;) {
-        const bool want = !retired && slot == kInvalid;
-        const uint32_t wmask = __ballot_sync(kFullMask, want);
-        if (wmask) {
-            const uint32_t leader = __ffs(wmask) - 1;
-            uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(queue, (uint32_t)__popc(wmask));
-            base = __shfl_sync(kFullMask, base, leader);
-            if (want) {
-                slot = base + __popc(wmask & lanemask_lt());
-                if (slot >= total) {
-                    slot = kInvalid;
-                    retired = true;
+        // refill stopped lanes with fresh leaves
+        uint32_t need = __ballot_sync(kFullMask, !active);
+        while (need && !exhausted) {
+            if (chunk_next == chunk_end) {
+                uint32_t b = 0;
+                if (lane == 0) b = atomicAdd(leaf_ctr, kLeafChunk);
+                b = __shfl_sync(kFullMask, b, 0);
+                if (b >= n) {
+                    exhausted = true;
+                    break;
                 }
+                chunk_next = b;
+                chunk_end = min(b + kLeafChunk, n);
             }
-        }
-        if (__all_sync(kFullMask, retired)) return;
-        uint32_t left = 0, right = 0;
-        bool ready = false;
-        if (slot < n) {
-            left = right = slot;
-            ready = true;
-        } else if (slot != kInvalid) {
-            const uint64_t t = ld_relaxed_u64(tasks + (slot - n));
-            if (t != ~0ull) {
-                left = (uint32_t)t;
-                right = (uint32_t)(t >> 32);
-                ready = true;
+            const uint32_t avail = chunk_end - chunk_next;
+            const uint32_t rank = __popc(need & lanemask_lt());
+            if (!active && ((need >> lane) & 1u) && rank < avail) {
+                left = right = chunk_next + rank;
+                active = true;
             }
+            const uint32_t took = min((uint32_t)__popc(need), avail);
+            chunk_next += took;
+            need = __ballot_sync(kFullMask, !active);
         }
-        if (!__any_sync(kFullMask, ready)) {
-            if (++idle > kSpinLimit) {
-                if (lane == 0) set_error(err, NXB_DEVERR_HPLOC_QUEUE_TIMEOUT);
-                return;
-            }
-            __nanosleep(64);
-            continue;
-        }
-        idle = 0;
-        if (__any_sync(kFullMask, ready && slot >= n)) fence_acq_rel_gpu();
+        if (!__any_sync(kFullMask, active)) return;
         bool second = false;
-        uint32_t split = 0;
-        if (ready) {
-            slot = kInvalid;
-            if (left > right || right >= n) {
-                set_error(err, NXB_DEVERR_HPLOC_INVALID_CLUSTER);
-            } else {
-                uint32_t prev;
-                const bool go_right =
-                    left == 0 || (right != n - 1 && delta(keys, right, right + 1) < delta(keys, left - 1, left));
-                if (go_right) {
-                    prev = atomicExch(parent + right, left);
-                    if (prev != kInvalid) {
-                        split = right + 1;
-                        right = prev;
-                    }
-                } else {
-                    prev = atomicExch(parent + left - 1, right);
-                    if (prev != kInvalid) {
-                        split = left;
-                        left = prev;
-                    }
+        if (active) {
+            uint32_t prev;
+            const bool go_right =
+                left == 0 || (right != n - 1 && delta(keys, right, right + 1) < delta(keys, left - 1, left));
+            if (go_right) {
+                prev = atomicExch(parent + right, left);
+                if (prev != kInvalid) {
+                    split = right + 1;
+                    right = prev;
                 }
-                second = prev != kInvalid;
+            } else {
+                prev = atomicExch(parent + left - 1, right);
+                if (prev != kInvalid) {
+                    split = left;
+                    left = prev;
+                }
             }
+            second = prev != kInvalid;
+            active = second;
         }
         const uint32_t size = right - left + 1;
         const bool final = second && size == n;
@@ -334,57 +313,43 @@ __global__ __launch_bounds__(kThreads) void hploc_kernel(const K* __restrict__ k
                 todo &= todo - 1;
             }
             __syncwarp();
-            fence_acq_rel_gpu();  // release: clusters and nodes before the pushes
-        }
-        const uint32_t pmask = __ballot_sync(kFullMask, second);
-        if (pmask) {
-            const uint32_t leader = __ffs(pmask) - 1;
-            uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(queue + 1, (uint32_t)__popc(pmask));
-            base = __shfl_sync(kFullMask, base, leader);
-            if (second) {
-                const uint32_t at = base + __popc(pmask & lanemask_lt());
-                if (at < n - 1)
-                    st_relaxed_u64(tasks + at, ((uint64_t)right << 32) | left);
-                else
-                    set_error(err, NXB_DEVERR_HPLOC_INVALID_CLUSTER);
-            }
+            fence_acq_rel_gpu();  // release: clusters and nodes before the next hand-over
         }
     }
 }
 
 template <typename K, int R>
 cudaError_t launch_r(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, uint32_t n, uint32_t* tok,
-                     uint32_t* pol, uint64_t* tasks, uint32_t* queue, uint32_t* err, cudaStream_t s) {
+                     uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err, cudaStream_t s) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hploc_kernel<K, R>, kThreads, 0);
     if (per_sm < 1) per_sm = 1;
-    const uint32_t want = (2 * n - 1 + kThreads - 1) / kThreads;
+    const uint32_t want = (n + kThreads - 1) / kThreads;
     const uint32_t grid = std::max(1u, std::min(want, (uint32_t)(device_info().sms * per_sm)));
-    hploc_kernel<K, R><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, n, tok, pol, tasks, queue, err);
+    hploc_kernel<K, R><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, n, tok, pol, leaf_ctr, err);
     return cudaGetLastError();
 }
 
 template <typename K>
 cudaError_t launch_t(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, uint32_t n, uint32_t radius,
-                     uint32_t* tok, uint32_t* pol, uint64_t* tasks, uint32_t* queue, uint32_t* err, cudaStream_t s) {
+                     uint32_t* tok, uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err, cudaStream_t s) {
     switch (radius) {
-        case 4: return launch_r<K, 4>(keys, cluster, parent, nodes, n, tok, pol, tasks, queue, err, s);
-        case 16: return launch_r<K, 16>(keys, cluster, parent, nodes, n, tok, pol, tasks, queue, err, s);
-        default: return launch_r<K, 8>(keys, cluster, parent, nodes, n, tok, pol, tasks, queue, err, s);
+        case 4: return launch_r<K, 4>(keys, cluster, parent, nodes, n, tok, pol, leaf_ctr, err, s);
+        case 16: return launch_r<K, 16>(keys, cluster, parent, nodes, n, tok, pol, leaf_ctr, err, s);
+        default: return launch_r<K, 8>(keys, cluster, parent, nodes, n, tok, pol, leaf_ctr, err, s);
     }
 }
 
 }  // namespace
 
 cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
-                         uint32_t n, uint32_t radius, uint32_t* tokens, uint32_t* parent_of_last, uint64_t* tasks,
-                         uint32_t* queue, uint32_t* err, cudaStream_t s) {
+                         uint32_t n, uint32_t radius, uint32_t* tokens, uint32_t* parent_of_last, uint32_t* leaf_ctr,
+                         uint32_t* err, cudaStream_t s) {
     if (key_bytes == 4)
         return launch_t<uint32_t>((const uint32_t*)keys, cluster_idx, parent, nodes, n, radius, tokens,
-                                  parent_of_last, tasks, queue, err, s);
+                                  parent_of_last, leaf_ctr, err, s);
     return launch_t<uint64_t>((const uint64_t*)keys, cluster_idx, parent, nodes, n, radius, tokens, parent_of_last,
-                              tasks, queue, err, s);
+                              leaf_ctr, err, s);
 }
 
 }  // namespace nxb

@@ -22,8 +22,8 @@ struct Control {
     uint32_t error_word;
     uint32_t bvh8_ctr[8];   // BVH8: slot claim, node counter, leaf counter, work-slot allocator, pending items
     uint32_t parent_of_last; // H-PLOC: the node whose child is node 2n-2 (seeded INVALID)
-    uint32_t hploc_queue[2]; // H-PLOC task queue: next slot to claim, next task to push
-    uint32_t pad[1];
+    uint32_t hploc_leaf_ctr; // H-PLOC: next unclaimed leaf
+    uint32_t pad[2];
     uint32_t tile_ctr[kMaxSortPasses];
     uint32_t hist[kMaxSortPasses][kRadixBins];
 };
@@ -84,11 +84,11 @@ cudaError_t launch_sort_pass(uint32_t key_bytes, const void* keys_in, void* keys
                              uint32_t* lookback, uint32_t* tile_ctr, uint32_t* err, cudaStream_t s);
 // ---------------------------------------------------------------- stage 4
 // tokens: n words of scratch (no initialisation needed); parent_of_last:
-// one word that must hold INVALID on entry; tasks: n-1 uint64 that must be
-// all ones on entry; queue: two words that must be zero on entry.
+// one word that must hold INVALID on entry; leaf_ctr: one word that must
+// be zero on entry.
 cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
-                         uint32_t n, uint32_t radius, uint32_t* tokens, uint32_t* parent_of_last, uint64_t* tasks,
-                         uint32_t* queue, uint32_t* err, cudaStream_t s);
+                         uint32_t n, uint32_t radius, uint32_t* tokens, uint32_t* parent_of_last, uint32_t* leaf_ctr,
+                         uint32_t* err, cudaStream_t s);
 // ---------------------------------------------------------------- stage 5
 // pairs: n uint64 slots; ctr: {claim, node, leaf, work}.  Both are
 // initialised by launch_bvh8_init (or the fused Morton seed + pair init).
