@@ -238,6 +238,29 @@ nxb_status nxb_stage_radix_sort(uint32_t key_bytes, const void* d_keys_in, void*
                                 void* d_scratch, size_t scratch_bytes, uint32_t* d_error_word,
                                 struct CUstream_st* stream);
 
+/* Stage 3 without caller scratch: this entry point has no counterpart in
+ * the reference.  It is for callers that cannot allocate device memory or
+ * pass this library a scratch buffer: for example a renderer rebuilding
+ * BVHs in its frame loop (cudaMalloc and cudaFree synchronise the whole
+ * device and stall the frame), or an engine whose device memory belongs to
+ * its own sub-allocator.  Same arguments and results as
+ * nxb_stage_radix_sort, minus the scratch: the scratch is a fixed array of
+ * about 3.7 MB inside the library, which every GPU that loads the library
+ * holds until the process exits.  It allocates nothing (no cudaMalloc,
+ * cudaFree or allocating library call).
+ *   - count may be at most NXB_NOALLOC_SORT_MAX_COUNT; larger counts return
+ *     NXB_ERR_UNSUPPORTED (use nxb_stage_radix_sort for those).
+ *   - The first call on a device looks up the array's device address with
+ *     that device current; make that first call before any stream capture.
+ *   - Every call, from any thread or stream, shares the one array: calls
+ *     whose work overlaps on the GPU race and corrupt each other's results.
+ *     Order them on one stream (or wait on the previous call's work). */
+#define NXB_NOALLOC_SORT_MAX_COUNT 262144u
+nxb_status nxb_stage_radix_sort_noalloc(uint32_t key_bytes, const void* d_keys_in, void* d_keys_out,
+                                        const uint32_t* d_vals_in, uint32_t* d_vals_out, uint32_t count,
+                                        uint32_t begin_bit, uint32_t end_bit, uint32_t* d_error_word,
+                                        struct CUstream_st* stream);
+
 /* Stage 4 (BuildBVH2Kernel): H-PLOC over sorted keys; d_cluster_idx is the
  * sorted permutation (it is overwritten); d_nodes leaves [0,n) must hold the
  * stage-1 output; internal nodes are written to [n, 2n-1).  Scratch:

@@ -272,6 +272,8 @@ nxb_status build_plain(const void* prims, nxb_prim_type type, uint32_t n, const 
 
 }  // namespace
 
+nxb_status record_cuda_error(cudaError_t e) { return cuda_fail(e); }
+
 const DeviceInfo& device_info() {
     static DeviceInfo infos[64];
     static bool ready[64] = {false};

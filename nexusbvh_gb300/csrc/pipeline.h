@@ -43,6 +43,9 @@ struct DeviceInfo {
 };
 const DeviceInfo& device_info();
 
+// Records e as this thread's last CUDA error and maps it to a status.
+nxb_status record_cuda_error(cudaError_t e);
+
 // ---------------------------------------------------------------- stage 1
 // Leaves + scene bounds; scene_ord (6 words, the Control::scene_ord
 // encoding) must be zero on entry.

@@ -15,6 +15,7 @@
 //   * keys are reordered in shared memory so that the global scatter writes
 //     runs of consecutive addresses.
 #include <algorithm>
+#include <mutex>
 
 #include "pipeline.h"
 
@@ -286,3 +287,96 @@ cudaError_t launch_sort_pass(uint32_t key_bytes, const void* keys_in, void* keys
 }
 
 }  // namespace nxb
+
+// ---------------------------------------------------------------------------
+// Radix sort with library-owned scratch (nxb_stage_radix_sort_noalloc).
+//
+// Some callers cannot hand this library a scratch buffer or let it allocate
+// one: a renderer that rebuilds BVHs inside its frame loop on a real-time
+// thread (cudaMalloc and cudaFree synchronise the whole device, which
+// stalls every other stream of the frame), an engine whose device memory is
+// owned by its own sub-allocator or budget, or a plugin that runs in a host
+// process it does not control.  For them the sort's scratch lives in a
+// fixed device array of this file, which every GPU that loads the library
+// keeps until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocAlign = 256;
+constexpr size_t align_na(size_t x) { return (x + kNoAllocAlign - 1) / kNoAllocAlign * kNoAllocAlign; }
+constexpr size_t kNoAllocHist = align_na(sizeof(uint32_t) * nxb::kMaxSortPasses * nxb::kRadixBins);
+constexpr size_t kNoAllocCtr = align_na(sizeof(uint32_t) * nxb::kMaxSortPasses);
+// one look-back word per (tile, digit, pass); the 64-bit tile is the smaller one
+constexpr size_t kNoAllocTiles =
+    (NXB_NOALLOC_SORT_MAX_COUNT + nxb::tile_keys<uint64_t>() - 1) / nxb::tile_keys<uint64_t>();
+constexpr size_t kNoAllocLookback = align_na(4ull * kNoAllocTiles * nxb::kRadixBins * nxb::kMaxSortPasses);
+constexpr size_t kNoAllocKeys = align_na(8ull * NXB_NOALLOC_SORT_MAX_COUNT);
+constexpr size_t kNoAllocVals = align_na(4ull * NXB_NOALLOC_SORT_MAX_COUNT);
+constexpr size_t kNoAllocZeroed = kNoAllocHist + kNoAllocCtr + kNoAllocLookback;
+constexpr size_t kNoAllocBytes = kNoAllocZeroed + kNoAllocKeys + kNoAllocVals;
+
+// The scratch itself (about 3.7 MB).  Host code must not pass this name to a
+// kernel: on the host it is only a stand-in for the symbol, not a device
+// address.  noalloc_scratch() looks up the real address per device.
+static __device__ __align__(256) unsigned char g_noalloc_sort_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch on the current device, looked up once per
+// device (with that device current) on its first call.
+cudaError_t noalloc_scratch(unsigned char** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_sort_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" nxb_status nxb_stage_radix_sort_noalloc(uint32_t key_bytes, const void* d_keys_in, void* d_keys_out,
+                                                   const uint32_t* d_vals_in, uint32_t* d_vals_out, uint32_t count,
+                                                   uint32_t begin_bit, uint32_t end_bit, uint32_t* d_error_word,
+                                                   struct CUstream_st* stream) {
+    using namespace nxb;
+    if (key_bytes != 4 && key_bytes != 8) return NXB_ERR_UNSUPPORTED;
+    if (begin_bit >= end_bit || end_bit > key_bytes * 8) return NXB_ERR_INVALID_ARGUMENT;
+    if (!d_keys_in || !d_keys_out || !d_vals_out || count == 0) return NXB_ERR_INVALID_ARGUMENT;
+    if (count > NXB_NOALLOC_SORT_MAX_COUNT) return NXB_ERR_UNSUPPORTED;  // larger sorts: nxb_stage_radix_sort
+    unsigned char* base = nullptr;
+    cudaError_t e = noalloc_scratch(&base);
+    if (e != cudaSuccess) return record_cuda_error(e);
+    const SortPlan plan = make_sort_plan(begin_bit, end_bit);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(base);
+    uint32_t* ctr = reinterpret_cast<uint32_t*>(base + kNoAllocHist);
+    uint32_t* lookback = reinterpret_cast<uint32_t*>(base + kNoAllocHist + kNoAllocCtr);
+    void* keys_tmp = base + kNoAllocZeroed;
+    uint32_t* vals_tmp = reinterpret_cast<uint32_t*>(base + kNoAllocZeroed + kNoAllocKeys);
+    // the histograms, tile counters and look-back flags of the previous call
+    // are still there: clear them
+    e = cudaMemsetAsync(base, 0, kNoAllocZeroed, stream);
+    if (e == cudaSuccess) e = launch_sort_histogram(key_bytes, d_keys_in, count, plan, hist, stream);
+    const size_t per_pass = sort_lookback_words(count, key_bytes, 1);
+    const void* kin = d_keys_in;
+    const uint32_t* vin = d_vals_in;
+    for (int p = 0; p < plan.passes && e == cudaSuccess; ++p) {
+        const bool last_is_out = ((plan.passes - 1 - p) % 2) == 0;
+        void* kout = last_is_out ? d_keys_out : keys_tmp;
+        uint32_t* vout = last_is_out ? d_vals_out : vals_tmp;
+        e = launch_sort_pass(key_bytes, kin, kout, vin, vout, count, plan.shift[p], plan.bits[p],
+                             hist + p * kRadixBins, lookback + p * per_pass, ctr + p, d_error_word, stream);
+        kin = kout;
+        vin = vout;
+    }
+    return e == cudaSuccess ? NXB_OK : record_cuda_error(e);
+}
