@@ -46,6 +46,8 @@ WORKLOADS = {
     "clustered12m": ("clustered12m: 12,582,912 triangles, 256 anisotropic Gaussians, lognormal(-6,1) edges", 63),
     "sphere4m": ("sphere4m: 4,194,304 triangles, 2048x1024 displaced UV sphere", 63),
     "soup65k": ("soup65k: 65,536 triangles, uniform centroids, +-0.005 vertex offsets", 30),
+    "clustered4m": ("clustered4m: 4,194,304 triangles, the clustered12m generator at a third of the size "
+                    "(profiling case)", 63),
 }
 
 # Algorithmic bytes per triangle of each stage (k = key bytes, P = passes):

@@ -94,4 +94,6 @@ def by_name(name: str) -> np.ndarray:
         return displaced_sphere()
     if name == "clustered12m":
         return clustered()
+    if name == "clustered4m":
+        return clustered(4_194_304)
     raise KeyError(name)
