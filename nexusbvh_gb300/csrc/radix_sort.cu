@@ -67,7 +67,7 @@ __device__ __forceinline__ uint32_t cta_exclusive_scan(uint32_t v, uint32_t* s_t
 }
 
 template <typename K, bool HAS_VALS>
-__global__ __launch_bounds__(kThreads) void onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout,
+__global__ __launch_bounds__(kThreads, 4) void onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout,
                                                             const uint32_t* __restrict__ vin,
                                                             uint32_t* __restrict__ vout, uint32_t n, uint32_t shift,
                                                             uint32_t bits, const uint32_t* __restrict__ hist,
@@ -214,6 +214,9 @@ cudaError_t launch_pass_t(const K* kin, K* kout, const uint32_t* vin, uint32_t* 
     if (!configured) {
         cudaFuncSetAttribute(onesweep_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(onesweep_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        // four tiles per SM: shared memory, not L1, gets the carveout
+        cudaFuncSetAttribute(onesweep_kernel<K, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        cudaFuncSetAttribute(onesweep_kernel<K, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         configured = true;
     }
     const uint32_t tiles = (n + tile_keys<K>() - 1) / tile_keys<K>();

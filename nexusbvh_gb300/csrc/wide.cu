@@ -217,16 +217,27 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
     bool retired = false;
     uint32_t idle = 0;
     for (;;) {
-        // lanes without a slot claim the next ones, in increasing order
+        // lanes without a slot claim the next ones, in increasing order, but
+        // only slots a parent has already allocated (so they are ready, or
+        // about to be): a lane never sits on a slot of a subtree that does
+        // not exist yet while its warp's other lanes have work
         const bool want = !retired && slot == kInvalid;
         const uint32_t wmask = __ballot_sync(kFullMask, want);
         if (wmask) {
             const uint32_t leader = __ffs(wmask) - 1;
-            uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(ctr, (uint32_t)__popc(wmask));
+            uint32_t base = 0, got = 0;
+            if (lane == leader) {
+                const uint32_t claimed = ld_relaxed_u32(ctr);
+                const uint32_t alloc = ld_relaxed_u32(ctr + 3);
+                const uint32_t avail = alloc > claimed ? alloc - claimed : 0u;
+                got = min((uint32_t)__popc(wmask), avail);
+                if (got) base = atomicAdd(ctr, got);
+            }
             base = __shfl_sync(kFullMask, base, leader);
-            if (want) {
-                slot = base + __popc(wmask & lanemask_lt());
+            got = __shfl_sync(kFullMask, got, leader);
+            const uint32_t rank = __popc(wmask & lanemask_lt());
+            if (want && rank < got) {
+                slot = base + rank;
                 if (slot >= n) {
                     slot = kInvalid;
                     retired = true;
