@@ -551,7 +551,7 @@ nxb_status nxb_stage_hploc(uint32_t key_bytes, const void* d_sorted_keys, uint32
     return NXB_OK;
 }
 
-size_t nxb_bvh8_scratch_bytes(uint32_t n) { return align_up(8ull * n) + kAlign; }
+size_t nxb_bvh8_scratch_bytes(uint32_t n) { return align_up(8ull * n) + align_up(4 * kBvh8CtrWords); }
 
 nxb_status nxb_stage_bvh8(const nxb_bvh2_node* d_bvh2_nodes, uint32_t n, nxb_bvh8_node* d_bvh8_nodes,
                           uint32_t* d_prim_idx, uint32_t* d_counts, void* d_scratch, size_t scratch_bytes,
@@ -565,7 +565,8 @@ nxb_status nxb_stage_bvh8(const nxb_bvh2_node* d_bvh2_nodes, uint32_t n, nxb_bvh
     NXB_TRY(launch_bvh8_init(pairs, n, ctr, stream));
     NXB_TRY(launch_bvh8(reinterpret_cast<const Node2*>(d_bvh2_nodes), n, reinterpret_cast<Node8*>(d_bvh8_nodes),
                         (uint32_t)bvh8_capacity(n), d_prim_idx, pairs, ctr, d_error_word, stream));
-    NXB_TRY(cudaMemcpyAsync(d_counts, ctr + 1, 2 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
+    NXB_TRY(cudaMemcpyAsync(d_counts, ctr + kBvh8Nodes, sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
+    NXB_TRY(cudaMemcpyAsync(d_counts + 1, ctr + kBvh8Leaves, sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
     return NXB_OK;
 }
 

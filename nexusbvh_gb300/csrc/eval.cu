@@ -87,8 +87,8 @@ __global__ void finalize_kernel(const Control* ctrl, nxb_build_result* r, uint32
         r->scene_bounds.bmin[a] = ord2f(~ctrl->scene_ord[a]);
         r->scene_bounds.bmax[a] = ord2f(ctrl->scene_ord[3 + a]);
     }
-    r->bvh8_node_count = ctrl->bvh8_ctr[1];
-    r->bvh8_leaf_count = ctrl->bvh8_ctr[2];
+    r->bvh8_node_count = ctrl->bvh8_ctr[kBvh8Nodes];
+    r->bvh8_leaf_count = ctrl->bvh8_ctr[kBvh8Leaves];
     r->error_word = ctrl->error_word;
     r->bvh2_root = 2 * n - 2;
 }

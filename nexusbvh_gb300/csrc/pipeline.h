@@ -12,6 +12,12 @@
 namespace nxb {
 
 constexpr int kMaxSortPasses = 8;
+
+// BVH8 work-queue counters, each on its own 128-byte line (they are polled
+// and bumped by every warp): next slot to claim, BVH8 nodes, leaves, work
+// slots allocated, work items allocated but not finished.
+constexpr int kBvh8Claim = 0, kBvh8Nodes = 32, kBvh8Leaves = 64, kBvh8Alloc = 96, kBvh8Pending = 128;
+constexpr int kBvh8CtrWords = 160;
 constexpr int kRadixBits = 8;
 constexpr int kRadixBins = 1 << kRadixBits;
 
@@ -20,7 +26,8 @@ struct Control {
     uint32_t scene_ord[6];  // [0..2]: ~ordered(min) (atomicMax), [3..5]: ordered(max)
     uint32_t cluster_count; // H-PLOC node allocator
     uint32_t error_word;
-    uint32_t bvh8_ctr[8];   // BVH8: slot claim, node counter, leaf counter, work-slot allocator, pending items
+    uint32_t pad0[16];
+    alignas(128) uint32_t bvh8_ctr[160];  // BVH8 counters, one per 128-byte line (kBvh8* below)
     uint32_t parent_of_last; // H-PLOC: the node whose child is node 2n-2 (seeded INVALID)
     uint32_t hploc_leaf_ctr; // H-PLOC: next unclaimed leaf
     uint32_t pad[2];
@@ -93,8 +100,8 @@ cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster
                          uint32_t n, uint32_t radius, uint32_t* tokens, uint32_t* parent_of_last, uint32_t* leaf_ctr,
                          uint32_t* err, cudaStream_t s);
 // ---------------------------------------------------------------- stage 5
-// pairs: n uint64 slots; ctr: {claim, node, leaf, work}.  Both are
-// initialised by launch_bvh8_init (or the fused Morton seed + pair init).
+// pairs: n uint64 slots; ctr: kBvh8CtrWords words (128-byte aligned).
+// Both are initialised by launch_bvh8_init.
 cudaError_t launch_bvh8_init(uint64_t* pairs, uint32_t n, uint32_t* ctr, cudaStream_t s);
 cudaError_t launch_bvh8(const Node2* bvh2, uint32_t n, Node8* out, uint32_t cap, uint32_t* prim_idx, uint64_t* pairs,
                         uint32_t* ctr, uint32_t* err, cudaStream_t s);

@@ -180,23 +180,23 @@ __global__ void bvh8_init_kernel(uint64_t* pairs, uint32_t n, uint32_t* ctr) {
     for (uint32_t i = i0; i < n; i += gridDim.x * blockDim.x)
         pairs[i] = i == 0 ? ((uint64_t)(2 * n - 2) << 32) : ~0ull;
     if (i0 == 0) {
-        ctr[0] = 0;  // next work slot to claim
-        ctr[1] = 1;  // BVH8 nodes allocated (the root)
-        ctr[2] = 0;  // leaves allocated
-        ctr[3] = 1;  // work slots allocated (the root's)
-        ctr[4] = 1;  // work items allocated but not finished
+        ctr[kBvh8Claim] = 0;    // next work slot to claim
+        ctr[kBvh8Nodes] = 1;    // BVH8 nodes allocated (the root)
+        ctr[kBvh8Leaves] = 0;   // leaves allocated
+        ctr[kBvh8Alloc] = 1;    // work slots allocated (the root's)
+        ctr[kBvh8Pending] = 1;  // work items allocated but not finished
     }
 }
 
 // Work items are the internal BVH8 nodes only: a parent writes the
 // primitive of each leaf child straight into primIdx (it holds the leaf's
 // node in its slot table), instead of queueing a work item per leaf as the
-// reference does (one per primitive, each re-reading the leaf node).  A
-// parent's first inner child continues in the parent's own slot, the others
-// get fresh slots, so a slot is always written by an item in a lower slot.
-// Each lane holds one slot at a time and claims the next one (warp-
-// aggregated) as soon as its chain ends; the kernel ends when the count of
-// allocated-but-unfinished items drops to zero.
+// reference does (one per primitive, each re-reading the leaf node).  Every
+// inner child gets a fresh slot (breadth-first), so a slot is always written
+// by an item in a lower slot.  Each lane holds one slot at a time and claims
+// the next one (warp-aggregated) once its item is done, but only among the
+// slots already allocated, which are ready or about to be; the kernel ends
+// when the count of allocated-but-unfinished items drops to zero.
 __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict__ b2, uint32_t n, Node8* out,
                                                         uint32_t cap, uint32_t* prim_idx, uint64_t* pairs,
                                                         uint32_t* ctr, uint32_t* err) {
@@ -208,8 +208,8 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             write_node8(out, load_box(b2, 0), LeafZero{b2}, 0, 0, 0xFFFFFFF0u, 0u, 1u);
             prim_idx[0] = 0;
-            ctr[2] = 1;
-            ctr[4] = 0;
+            ctr[kBvh8Leaves] = 1;
+            ctr[kBvh8Pending] = 0;
         }
         return;
     }
@@ -227,11 +227,11 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
             const uint32_t leader = __ffs(wmask) - 1;
             uint32_t base = 0, got = 0;
             if (lane == leader) {
-                const uint32_t claimed = ld_relaxed_u32(ctr);
-                const uint32_t alloc = ld_relaxed_u32(ctr + 3);
+                const uint32_t claimed = ld_relaxed_u32(ctr + kBvh8Claim);
+                const uint32_t alloc = ld_relaxed_u32(ctr + kBvh8Alloc);
                 const uint32_t avail = alloc > claimed ? alloc - claimed : 0u;
                 got = min((uint32_t)__popc(wmask), avail);
-                if (got) base = atomicAdd(ctr, got);
+                if (got) base = atomicAdd(ctr + kBvh8Claim, got);
             }
             base = __shfl_sync(kFullMask, base, leader);
             got = __shfl_sync(kFullMask, got, leader);
@@ -253,12 +253,12 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
         }
         if (!__any_sync(kFullMask, ready)) {
             // nothing ready: finished when no allocated item is outstanding
-            if (ld_relaxed_u32(ctr + 4) == 0) return;
+            if (ld_relaxed_u32(ctr + kBvh8Pending) == 0) return;
             if (++idle > kQueueSpinLimit) {
                 if (lane == 0) set_error(err, NXB_DEVERR_BVH8_QUEUE_TIMEOUT);
                 return;
             }
-            __nanosleep(64);
+            __nanosleep(min(32u << min(idle, 5u), 1024u));  // back off: idle warps poll the counters
             continue;
         }
         idle = 0;
@@ -320,7 +320,7 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
         // warp-aggregated allocation of inner nodes, leaves and work slots
         const uint32_t ic = internal ? (uint32_t)__popc(inner) : 0u;
         const uint32_t lc = internal ? count - ic : 0u;
-        const uint32_t wc = ic > 0 ? ic - 1u : 0u;
+        const uint32_t wc = ic;  // every inner child becomes a work item of its own
         const uint32_t packed = ic | (lc << 10) | (wc << 20);
         uint32_t incl = packed;
 #pragma unroll
@@ -332,9 +332,9 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
         uint32_t bases[3] = {0, 0, 0};
         if (lane == 31) {
             const uint32_t tn = incl & 0x3FFu, tl = (incl >> 10) & 0x3FFu, tw = incl >> 20;
-            if (tn) bases[0] = atomicAdd(ctr + 1, tn);
-            if (tl) bases[1] = atomicAdd(ctr + 2, tl);
-            if (tw) bases[2] = atomicAdd(ctr + 3, tw);
+            if (tn) bases[0] = atomicAdd(ctr + kBvh8Nodes, tn);
+            if (tl) bases[1] = atomicAdd(ctr + kBvh8Leaves, tl);
+            if (tw) bases[2] = atomicAdd(ctr + kBvh8Alloc, tw);
         }
         const uint32_t nb = __shfl_sync(kFullMask, bases[0], 31);
         const uint32_t lb = __shfl_sync(kFullMask, bases[1], 31);
@@ -354,20 +354,20 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
                     if ((inner >> i) & 1u) {
                         const uint32_t k = popc_below(inner, i);
                         const uint64_t pair = ((uint64_t)tab.idx(a) << 32) | (child_base + k);
-                        st_relaxed_u64(pairs + (k == 0 ? slot : work_base + k - 1), pair);
+                        st_relaxed_u64(pairs + work_base + k, pair);
                     } else if ((leaf >> i) & 1u) {
                         prim_idx[prim_base + popc_below(leaf, i)] = tab.right(a);
                     }
                 }
                 write_node8(out + b8i, nd.b, tab, child_base, prim_base, asg, inner, leaf);
-                if (ic == 0) slot = kInvalid;
             }
+            slot = kInvalid;
         }
         // pending += items allocated - items finished (one atomic, so it can
         // only reach zero when no item is in flight)
         __syncwarp();
-        const uint32_t new_items = __shfl_sync(kFullMask, incl >> 20, 31) + __popc(__ballot_sync(kFullMask, ic > 0));
-        if (lane == 0 && new_items != done) atomicAdd(ctr + 4, new_items - done);
+        const uint32_t new_items = __shfl_sync(kFullMask, incl >> 20, 31);
+        if (lane == 0 && new_items != done) atomicAdd(ctr + kBvh8Pending, new_items - done);
     }
 }
 
@@ -387,19 +387,22 @@ cudaError_t configure_smem() {
 cudaError_t run_bvh8_stall_probe(uint32_t* err_out) {
     const uint32_t n = 2;
     unsigned char* buf = nullptr;
-    const size_t bytes = 3 * sizeof(Node2) + 2 * sizeof(Node8) + 8 * n + 4 * n + 64;
+    const size_t bytes = 4 * (kBvh8CtrWords + 32) + 3 * sizeof(Node2) + 2 * sizeof(Node8) + 8 * n + 4 * n;
     cudaError_t e = configure_smem();
     if (!e) e = cudaMalloc(&buf, bytes);
     if (e) return e;
-    Node2* b2 = (Node2*)buf;
-    Node8* out = (Node8*)(buf + 3 * sizeof(Node2));
-    uint64_t* pairs = (uint64_t*)(buf + 3 * sizeof(Node2) + 2 * sizeof(Node8));
+    uint32_t* ctr = (uint32_t*)buf;  // 256-byte aligned
+    uint32_t* err = ctr + kBvh8CtrWords;
+    Node2* b2 = (Node2*)(buf + 4 * (kBvh8CtrWords + 32));
+    Node8* out = (Node8*)(b2 + 3);
+    uint64_t* pairs = (uint64_t*)(out + 2);
     uint32_t* prim = (uint32_t*)(pairs + n);
-    uint32_t* ctr = prim + n;
-    uint32_t* err = ctr + 5;
     e = cudaMemset(buf, 0, bytes);
     if (!e) e = cudaMemset(pairs, 0xFF, 8 * n);
-    const uint32_t c[6] = {0, 1, 0, 1, 1, 0};  // pending = 1: the never-seeded root
+    uint32_t c[kBvh8CtrWords] = {};
+    c[kBvh8Nodes] = 1;
+    c[kBvh8Alloc] = 1;    // slot 0 is allocated ...
+    c[kBvh8Pending] = 1;  // ... but its pair is never written
     if (!e) e = cudaMemcpy(ctr, c, sizeof(c), cudaMemcpyHostToDevice);
     if (!e) {
         bvh8_kernel<<<1, kThreads, kSlotSmem>>>(b2, n, out, 2, prim, pairs, ctr, err);
