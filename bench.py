@@ -2,7 +2,8 @@
 """Benchmark of the full BVH build (bounds -> Morton -> sort -> H-PLOC -> BVH8).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload clustered12m|sphere4m|soup65k] [--key-bits 30|63]
+                    [--workload clustered12m|sphere4m|soup65k|clustered4m|batch1024]
+                    [--key-bits 30|63]
                     [--radius 4|8|16]
 
 One step = one complete build of the workload.  The default workload is the
@@ -48,7 +49,10 @@ WORKLOADS = {
     "soup65k": ("soup65k: 65,536 triangles, uniform centroids, +-0.005 vertex offsets", 30),
     "clustered4m": ("clustered4m: 4,194,304 triangles, the clustered12m generator at a third of the size "
                     "(profiling case)", 63),
+    "batch1024": ("batch1024: 1024 meshes, n log-U[256, 262144] (36,469,370 triangles), each a uniform soup in "
+                  "its own box (origin U[-100,100]^3, extent log-U[0.1,10])", 30),
 }
+BATCH_WORKLOADS = {"batch1024": (1024, 3)}
 
 # Algorithmic bytes per triangle of each stage (k = key bytes, P = passes):
 # bounds R36+W32; Morton R24 + W k + W4; sort 2P(k+4)+k; H-PLOC k+72;
@@ -313,6 +317,168 @@ def run_ours(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args, world, rank, local):
+    """Batched form: all meshes in one graph-replayed pipeline (nxb_batch_*),
+    next to a loop of plain builds over the same meshes."""
+    import torch
+    import nexusbvh_gb300 as nxb
+    from nexusbvh_gb300 import scenes
+
+    torch.cuda.set_device(local)
+    lib = nxb.load()
+    meshes, seed = BATCH_WORKLOADS[args.workload]
+    counts = scenes.batch_counts(meshes, seed=seed)
+    prims_np = scenes.batch_meshes(counts, seed=seed)
+    n = prims_np.shape[0]
+    off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    d_prims = torch.from_numpy(prims_np).cuda()
+    stream = torch.cuda.current_stream()
+    sptr = int(stream.cuda_stream)
+    batch = nxb.Batch(counts, config=nxb.BuildConfig(prioritize_speed=True, search_radius=args.radius))
+    t_tune = time.perf_counter()
+    tuning = batch.autotune(d_prims, repeats=2)
+    t_tune = time.perf_counter() - t_tune
+    for _ in range(args.warmup):
+        batch.build_async(d_prims)
+    batch.wait(results=False)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        start.record(stream)
+        for _ in range(args.steps):
+            batch.build_async(d_prims)
+        stop.record(stream)
+        torch.cuda.synchronize()
+    res = batch.wait(results=True)
+    elapsed = start.elapsed_time(stop)
+    if world > 1:
+        t = torch.tensor([elapsed], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = world * n * args.steps / elapsed / 1e3
+    n8 = sum(r.bvh8_node_count for r in res)
+
+    # e2e: pinned host triangles -> device, batch build, per-mesh results back
+    h_prims = torch.from_numpy(prims_np).pin_memory()
+    d_in = torch.empty_like(d_prims)
+    d_in.copy_(h_prims, non_blocking=True)
+    batch.build(d_in)  # capture for this buffer
+    e2e_steps = max(3, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        d_in.copy_(h_prims, non_blocking=True)
+        batch.build(d_in)
+    e2e_s = time.perf_counter() - t0
+    e2e_value = world * n * e2e_steps / e2e_s / 1e6
+
+    # the loop of plain builds the batch replaces: the reference-shaped call
+    # per mesh (allocating, synchronising), and nxb_build_async per mesh into
+    # one resident workspace (no per-mesh synchronisation)
+    cfg = nxb.BuildConfig(prioritize_speed=True, search_radius=args.radius)
+    c = cfg.to_c()
+    out = nxb.CBVH8()
+
+    def loop_plain():
+        for m in range(meshes):
+            k = int(counts[m])
+            if k == 0:
+                continue
+            ptr = d_prims.data_ptr() + int(off[m]) * 36
+            nxb.check(lib.nxb_build_bvh8(ptr, nxb.NXB_PRIM_TRIANGLE, k, ctypes.byref(c), sptr, ctypes.byref(out),
+                                         None), "nxb_build_bvh8")
+            nxb.check(lib.nxb_free_device_bvh8(ctypes.byref(out)), "nxb_free_device_bvh8")
+
+    b = nxb.Builder()
+    big = int(max(counts))
+    sz = b.sizes(big, cfg)
+    ws = b.workspace(sz.workspace_bytes)
+    b2 = torch.empty((sz.bvh2_node_count, 32), dtype=torch.uint8, device="cuda")
+    b8 = torch.empty((sz.bvh8_node_capacity, 80), dtype=torch.uint8, device="cuda")
+    pidx = torch.empty(big, dtype=torch.int32, device="cuda")
+    rbuf = torch.zeros(64, dtype=torch.uint8, device="cuda")
+
+    def loop_async():
+        for m in range(meshes):
+            k = int(counts[m])
+            if k == 0:
+                continue
+            ptr = d_prims.data_ptr() + int(off[m]) * 36
+            nxb.check(lib.nxb_build_async(ptr, nxb.NXB_PRIM_TRIANGLE, k, ctypes.byref(c), ws.data_ptr(), ws.numel(),
+                                          b2.data_ptr(), b8.data_ptr(), pidx.data_ptr(), rbuf.data_ptr(), sptr),
+                      "nxb_build_async")
+
+    loop_plain()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loop_plain()
+    torch.cuda.synchronize()
+    t_loop = time.perf_counter() - t0
+    loop_async()
+    torch.cuda.synchronize()
+    start.record(stream)
+    loop_async()
+    stop.record(stream)
+    torch.cuda.synchronize()
+    t_loop_async = start.elapsed_time(stop) / 1e3
+    if rank != 0:
+        return
+    pk = peaks()
+    passes = -(-(30 + max(1, (meshes - 1).bit_length())) // int(tuning.sort_digit_bits))
+    per_tri = (algorithmic_bytes("scene_bounds", 8, passes, 0) + algorithmic_bytes("morton", 8, passes, 0)
+               + 4.0 + algorithmic_bytes("radix_sort", 8, passes, 0) + algorithmic_bytes("hploc", 8, passes, 0)
+               + algorithmic_bytes("bvh8", 8, passes, n8 / n))
+    ms = elapsed / args.steps
+    gbs = per_tri * n / (ms * 1e-3) / 1e9
+    line = {
+        "metric": "Mtris/s batched build (1024 meshes, bounds, Morton, radix sort, H-PLOC BVH2, BVH8)",
+        "value": round(value, 2), "unit": "Mtris/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded generators standing in for the reference's scene files)",
+        "config": {
+            "workload": WORKLOADS[args.workload][0], "meshes": meshes, "n_tris": n, "key_bits": 30,
+            "search_radius": int(tuning.search_radius), "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (1.3 GB of triangles), no flush needed",
+            "tuning": {"sort_digit_bits": int(tuning.sort_digit_bits), "sort_passes": passes,
+                       "hploc_ctas_per_sm": int(tuning.hploc_ctas_per_sm),
+                       "candidates": int(tuning.candidates_tried), "tune_s": round(t_tune, 2)},
+            "bvh8_nodes": int(n8),
+            "loop_plain_api_ms": round(t_loop * 1e3, 2),
+            "loop_plain_api_mtris_s": round(n / t_loop / 1e6, 2),
+            "loop_async_ms": round(t_loop_async * 1e3, 2),
+            "speedup_vs_loop_plain_api": round(t_loop * 1e3 / ms, 2),
+            "speedup_vs_loop_async": round(t_loop_async * 1e3 / ms, 2),
+        },
+        "roofline": {"kernel": "whole batched pipeline", "bound": "hbm", "achieved": round(gbs, 1),
+                     "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(gbs / pk["hbm_gbs"], 3), "traffic": None,
+                     "peak_source": pk["source"]},
+        "e2e": {"value": round(e2e_value, 2), "unit": "Mtris/s", "h2d_bytes_per_step": 36 * n,
+                "d2h_bytes_per_step": 52 * meshes + 4,
+                "call": "nxb_batch_build (graph replay + wait + per-mesh results) after a pinned host->device copy"},
+        "gpu_launches": (6 + passes) * args.steps,
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu_baseline:
+        import oracle
+        t = time.perf_counter()
+        done = 0
+        m = 0
+        while done < args.cpu_sample and m < meshes:
+            k = int(counts[m])
+            if k:
+                r = oracle.build(np.ascontiguousarray(prims_np[off[m]:off[m + 1]]), 30, args.radius)
+                assert r["err"] == 0
+                done += k
+            m += 1
+        dt = time.perf_counter() - t
+        line["cpu_baseline"] = {"value": round(done / dt / 1e6, 3), "unit": "Mtris/s", "cores": oracle.threads(),
+                                "kind": "port", "sample": f"the first {m} meshes ({done:,} triangles), one CPU build "
+                                                          f"each, in {dt:.2f} s"}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, world, rank, local):
     """The reference arm.  The reference's path has no CPU implementation,
     and its own CUDA build is not run on the GPU any more: its H-PLOC kernel
@@ -326,21 +492,34 @@ def run_reference(args, world, rank, local):
         return
     import oracle
 
-    prims_np = make_prims(args.workload)
-    n = prims_np.shape[0]
     key_bits = args.key_bits
-    m = min(args.cpu_sample, n)
-    sub = np.ascontiguousarray(prims_np[:m])
+    if args.workload in BATCH_WORKLOADS:
+        from nexusbvh_gb300 import scenes
+        meshes, seed = BATCH_WORKLOADS[args.workload]
+        counts = scenes.batch_counts(meshes, seed=seed)
+        prims_np = scenes.batch_meshes(counts, seed=seed)
+        off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+        # a prefix of whole meshes, each built on its own
+        last = int(np.searchsorted(off, min(args.cpu_sample, off[-1]), side="left"))
+        last = max(1, min(last, meshes))
+        subs = [np.ascontiguousarray(prims_np[off[i]:off[i + 1]]) for i in range(last) if counts[i]]
+    else:
+        prims_np = make_prims(args.workload)
+        subs = [np.ascontiguousarray(prims_np[:min(args.cpu_sample, prims_np.shape[0])])]
+    n = prims_np.shape[0]
+    m = sum(x.shape[0] for x in subs)
+    sub = subs[0]
     for _ in range(args.warmup):
-        oracle.build(sub[: min(m, 65536)], key_bits, args.radius)
+        oracle.build(sub[: min(sub.shape[0], 65536)], key_bits, args.radius)
     times = []
     stage = np.zeros(5)
     for _ in range(args.steps):
         t = time.perf_counter()
-        r = oracle.build(sub, key_bits, args.radius)
+        for x in subs:
+            r = oracle.build(x, key_bits, args.radius)
+            assert r["err"] == 0
+            stage += np.array(r["stage_ms"])
         times.append(time.perf_counter() - t)
-        assert r["err"] == 0
-        stage += np.array(r["stage_ms"])
     total = sum(times)
     value = m * args.steps / total / 1e6
     line = {"metric": "Mtris/s full build (bounds, Morton, radix sort, H-PLOC BVH2, BVH8)", "value": round(value, 3),
@@ -383,6 +562,8 @@ def main():
     try:
         if args.impl == "reference":
             run_reference(args, world, rank, local)
+        elif args.workload in BATCH_WORKLOADS:
+            run_batch(args, world, rank, local)
         else:
             run_ours(args, world, rank, local)
     finally:

@@ -290,6 +290,80 @@ nxb_status nxb_eval_bvh8_cost(const nxb_bvh8_node* d_nodes, uint32_t node_count,
                               const nxb_aabb* d_root_bounds, float* d_cost,
                               struct CUstream_st* stream);
 
+/* ------------------------------------------------------------ batched builds */
+/* No counterpart in the reference's API, which builds one mesh per call
+ * (NXB::BuildBVH8, NexusBVH/include/NXB/BVHBuilder.h:18-31).  A batch builds
+ * many independent meshes, concatenated in one device array, with one
+ * launch per stage over all of them, replayed from a CUDA graph.  Each mesh
+ * is built exactly as a plain build of that mesh alone would build it (own
+ * scene box, same Morton codes, same sort order, same H-PLOC decisions, same
+ * BVH8 collapse): only BVH8 node numbering differs, as it does between two
+ * plain builds.  Batches use 30-bit Morton codes (config->prioritize_speed
+ * must be nonzero).  Results live in batch-owned device memory, valid until
+ * the next build of the batch or nxb_batch_destroy. */
+typedef struct nxb_batch nxb_batch; /* opaque */
+
+typedef struct nxb_batch_mesh {        /* per-mesh result, 52 B */
+    nxb_aabb scene_bounds;             /* this mesh's own scene box */
+    uint32_t prim_offset, prim_count;  /* its primitives in the input; its prim_idx slice */
+    uint32_t bvh2_offset;              /* its BVH2 nodes start here (leaves first, root at +2n-2) */
+    uint32_t bvh2_node_count;          /* 2n-1 (0 for an empty mesh) */
+    uint32_t bvh8_offset;              /* its BVH8 nodes start here, root first */
+    uint32_t bvh8_node_count, bvh8_leaf_count;
+} nxb_batch_mesh;
+
+typedef struct nxb_batch_arrays {      /* device views owned by the batch */
+    const nxb_bvh2_node* bvh2_nodes;   /* child indices are mesh-local */
+    const nxb_bvh8_node* bvh8_nodes;   /* child_base / prim_base are mesh-local */
+    const uint32_t* prim_idx;          /* mesh-local primitive indices */
+    const nxb_batch_mesh* meshes;      /* [mesh_count], written by every build */
+    uint32_t mesh_count;
+    uint32_t prim_count;
+    size_t bvh2_node_capacity, bvh8_node_capacity;
+} nxb_batch_arrays;
+
+typedef struct nxb_batch_tuning {
+    uint32_t sort_digit_bits;   /* 5..8: bits per radix sort pass */
+    uint32_t search_radius;     /* H-PLOC radius in use */
+    uint32_t hploc_ctas_per_sm; /* cap on the H-PLOC persistent grid (0 = occupancy) */
+    uint32_t candidates_tried;
+    float build_ms;             /* median time of one build with these settings */
+} nxb_batch_tuning;
+
+/* Tuning flags for nxb_batch_autotune. */
+#define NXB_TUNE_RADIUS 0x1u /* also try radius 4, 8 and 16: this changes the trees */
+
+/* Creates a batch for mesh_count meshes whose primitive counts are given as
+ * a host prefix array h_prim_offsets[0..mesh_count] (h_prim_offsets[0] = 0,
+ * non-decreasing; empty meshes allowed).  Allocates all device memory the
+ * batch needs on the current device (one allocation). */
+nxb_status nxb_batch_create(nxb_prim_type prim_type, const uint32_t* h_prim_offsets, uint32_t mesh_count,
+                            const nxb_build_config* config, nxb_batch** out_batch);
+nxb_status nxb_batch_destroy(nxb_batch* batch);
+/* Enqueues one build of the batch from d_prims (all meshes' primitives end
+ * to end) on `stream`: a graph launch, nothing else (the graph is captured
+ * on the first call and again when d_prims or the tuning changes).  No host
+ * synchronisation; nxb_batch_wait reports the outcome. */
+nxb_status nxb_batch_build_async(nxb_batch* batch, const void* d_prims, struct CUstream_st* stream);
+/* Waits for `stream`, checks the device error word and, if h_meshes is not
+ * NULL, copies the mesh_count per-mesh results into it. */
+nxb_status nxb_batch_wait(nxb_batch* batch, struct CUstream_st* stream, nxb_batch_mesh* h_meshes);
+/* nxb_batch_build_async + nxb_batch_wait. */
+nxb_status nxb_batch_build(nxb_batch* batch, const void* d_prims, struct CUstream_st* stream,
+                           nxb_batch_mesh* h_meshes);
+nxb_status nxb_batch_get_arrays(const nxb_batch* batch, nxb_batch_arrays* out_arrays);
+/* Times candidate settings on this batch and input (each: one warm-up build,
+ * then the median of `repeats` builds) and keeps the fastest.  Without
+ * NXB_TUNE_RADIUS only settings that leave the results unchanged are tried
+ * (sort digit width, H-PLOC grid size). */
+nxb_status nxb_batch_autotune(nxb_batch* batch, const void* d_prims, uint32_t tune_flags, uint32_t repeats,
+                              struct CUstream_st* stream, nxb_batch_tuning* out_choice);
+nxb_status nxb_batch_set_tuning(nxb_batch* batch, const nxb_batch_tuning* tuning);
+nxb_status nxb_batch_get_tuning(const nxb_batch* batch, nxb_batch_tuning* out_tuning);
+/* Host copy of one mesh's BVH8 (like nxb_bvh8_to_host; free with
+ * nxb_free_host_bvh8) after a successful build. */
+nxb_status nxb_batch_mesh_bvh8_to_host(const nxb_batch* batch, uint32_t mesh, nxb_bvh8* host_bvh);
+
 /* Library version and the compile flags that define its numerics. */
 const char* nxb_version(void);
 

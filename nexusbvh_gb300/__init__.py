@@ -82,7 +82,28 @@ class CResult(ctypes.Structure):
                 ("error_word", ctypes.c_uint32), ("bvh2_root", ctypes.c_uint32)]
 
 
+class CBatchMesh(ctypes.Structure):
+    _fields_ = [("scene_bounds", CAABB), ("prim_offset", ctypes.c_uint32), ("prim_count", ctypes.c_uint32),
+                ("bvh2_offset", ctypes.c_uint32), ("bvh2_node_count", ctypes.c_uint32),
+                ("bvh8_offset", ctypes.c_uint32), ("bvh8_node_count", ctypes.c_uint32),
+                ("bvh8_leaf_count", ctypes.c_uint32)]
+
+
+class CBatchArrays(ctypes.Structure):
+    _fields_ = [("bvh2_nodes", ctypes.c_void_p), ("bvh8_nodes", ctypes.c_void_p), ("prim_idx", ctypes.c_void_p),
+                ("meshes", ctypes.c_void_p), ("mesh_count", ctypes.c_uint32), ("prim_count", ctypes.c_uint32),
+                ("bvh2_node_capacity", ctypes.c_size_t), ("bvh8_node_capacity", ctypes.c_size_t)]
+
+
+class CBatchTuning(ctypes.Structure):
+    _fields_ = [("sort_digit_bits", ctypes.c_uint32), ("search_radius", ctypes.c_uint32),
+                ("hploc_ctas_per_sm", ctypes.c_uint32), ("candidates_tried", ctypes.c_uint32),
+                ("build_ms", ctypes.c_float)]
+
+
 assert ctypes.sizeof(CBVH2) == 40 and ctypes.sizeof(CBVH8) == 56 and ctypes.sizeof(CMetrics) == 36
+assert ctypes.sizeof(CBatchMesh) == 52
+NXB_TUNE_RADIUS = 0x1
 
 _P = ctypes.c_void_p
 _U32 = ctypes.c_uint32
@@ -114,6 +135,16 @@ _SIG = {
     "nxb_eval_bvh8_cost": (ctypes.c_int, [_P, _U32, _P, _P, _P]),
     "nxb_selftest_numerics": (ctypes.c_int, [_P, _U32]),
     "nxb_selftest_bounded_waits": (ctypes.c_int, [_P]),
+    "nxb_batch_create": (ctypes.c_int, [ctypes.c_int, _P, _U32, _P, ctypes.POINTER(ctypes.c_void_p)]),
+    "nxb_batch_destroy": (ctypes.c_int, [_P]),
+    "nxb_batch_build_async": (ctypes.c_int, [_P, _P, _P]),
+    "nxb_batch_wait": (ctypes.c_int, [_P, _P, _P]),
+    "nxb_batch_build": (ctypes.c_int, [_P, _P, _P, _P]),
+    "nxb_batch_get_arrays": (ctypes.c_int, [_P, ctypes.POINTER(CBatchArrays)]),
+    "nxb_batch_autotune": (ctypes.c_int, [_P, _P, _U32, _U32, _P, ctypes.POINTER(CBatchTuning)]),
+    "nxb_batch_set_tuning": (ctypes.c_int, [_P, ctypes.POINTER(CBatchTuning)]),
+    "nxb_batch_get_tuning": (ctypes.c_int, [_P, ctypes.POINTER(CBatchTuning)]),
+    "nxb_batch_mesh_bvh8_to_host": (ctypes.c_int, [_P, _U32, ctypes.POINTER(CBVH8)]),
 }
 
 
@@ -321,6 +352,96 @@ def _borrow(ptr: int, nbytes: int):
     obj.__cuda_array_interface__ = {"shape": (nbytes,), "typestr": "|u1", "data": (ptr, False), "version": 3,
                                     "strides": None}
     return torch.as_tensor(obj, device="cuda")
+
+
+class Batch:
+    """Batched builds of many independent meshes (``nxb_batch_*``).
+
+    ``counts`` are the meshes' primitive counts; ``build(prims)`` takes all
+    meshes' primitives end to end in one CUDA tensor and builds every mesh
+    exactly as ``build_bvh8`` would build it alone (30-bit codes only).
+    """
+
+    def __init__(self, counts, prim_type: int = NXB_PRIM_TRIANGLE, config: BuildConfig | None = None):
+        lib = load()
+        config = config or BuildConfig(prioritize_speed=True)
+        counts = np.asarray(counts, dtype=np.uint64)
+        off = np.zeros(len(counts) + 1, dtype=np.uint32)
+        off[1:] = np.cumsum(counts).astype(np.uint32)
+        self.offsets = off
+        self.mesh_count = len(counts)
+        self._handle = ctypes.c_void_p()
+        c = config.to_c()
+        check(lib.nxb_batch_create(prim_type, off.ctypes.data, self.mesh_count, ctypes.byref(c),
+                                   ctypes.byref(self._handle)), "nxb_batch_create")
+
+    def close(self) -> None:
+        if self._handle:
+            load().nxb_batch_destroy(self._handle)
+            self._handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def build_async(self, prims, stream=None) -> None:
+        check(load().nxb_batch_build_async(self._handle, prims.data_ptr(), _stream_ptr(stream)),
+              "nxb_batch_build_async")
+
+    def wait(self, stream=None, results: bool = True):
+        meshes = (CBatchMesh * self.mesh_count)() if results else None
+        check(load().nxb_batch_wait(self._handle, _stream_ptr(stream),
+                                    ctypes.cast(meshes, ctypes.c_void_p) if results else None), "nxb_batch_wait")
+        return list(meshes) if results else None
+
+    def build(self, prims, stream=None):
+        self.build_async(prims, stream)
+        return self.wait(stream)
+
+    def autotune(self, prims, flags: int = 0, repeats: int = 3, stream=None) -> CBatchTuning:
+        t = CBatchTuning()
+        check(load().nxb_batch_autotune(self._handle, prims.data_ptr(), flags, repeats, _stream_ptr(stream),
+                                        ctypes.byref(t)), "nxb_batch_autotune")
+        return t
+
+    def tuning(self) -> CBatchTuning:
+        t = CBatchTuning()
+        check(load().nxb_batch_get_tuning(self._handle, ctypes.byref(t)), "nxb_batch_get_tuning")
+        return t
+
+    def set_tuning(self, t: CBatchTuning) -> None:
+        check(load().nxb_batch_set_tuning(self._handle, ctypes.byref(t)), "nxb_batch_set_tuning")
+
+    def arrays(self) -> CBatchArrays:
+        a = CBatchArrays()
+        check(load().nxb_batch_get_arrays(self._handle, ctypes.byref(a)), "nxb_batch_get_arrays")
+        return a
+
+    def mesh_bvh8_host(self, mesh: int):
+        """(nodes as BVH8_NODE_DTYPE array, prim_idx uint32 array) of one mesh."""
+        lib = load()
+        h = CBVH8()
+        check(lib.nxb_batch_mesh_bvh8_to_host(self._handle, mesh, ctypes.byref(h)), "nxb_batch_mesh_bvh8_to_host")
+        try:
+            nodes = np.frombuffer(ctypes.string_at(h.nodes, h.node_count * 80), dtype=BVH8_NODE_DTYPE).copy()
+            prim = np.frombuffer(ctypes.string_at(h.prim_idx, h.prim_count * 4), dtype=np.uint32).copy()
+        finally:
+            lib.nxb_free_host_bvh8(ctypes.byref(h))
+        return nodes, prim
+
+    def mesh_bvh2_host(self, mesh: int, meshes=None):
+        """BVH2 nodes (BVH2_NODE_DTYPE, mesh-local child indices) of one mesh after a build."""
+        import torch
+        a = self.arrays()
+        info = (meshes or self.wait(results=True))[mesh]
+        nbytes = info.bvh2_node_count * 32
+        if nbytes == 0:
+            return np.zeros(0, dtype=BVH2_NODE_DTYPE)
+        t = _borrow(a.bvh2_nodes + info.bvh2_offset * 32, nbytes)
+        torch.cuda.synchronize()
+        return np.frombuffer(t.cpu().numpy().tobytes(), dtype=BVH2_NODE_DTYPE).copy()
 
 
 def selftest_numerics() -> list[int]:

@@ -175,4 +175,52 @@ __device__ __forceinline__ void set_error(uint32_t* err, uint32_t bit) {
     if (err) atomicOr(err, bit);
 }
 
+// ------------------------------------------------------------ mesh batches
+// The largest m in [lo, hi] with off[m] <= x.  With off a prefix array of
+// element counts, this is the mesh that owns element x (empty meshes repeat
+// an offset and are skipped).
+__device__ __forceinline__ uint32_t owner_of(const uint32_t* off, uint32_t lo, uint32_t hi, uint32_t x) {
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (__ldg(off + mid) <= x)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// Sort key of a batched 30-bit build: mesh index << 32 | Morton code.
+struct MeshKey {
+    uint64_t v;
+};
+
+// One mesh of a build: its index, its first element in the concatenated
+// arrays and its primitive count.
+struct MeshSpan {
+    uint32_t m, start, count;
+};
+
+// A plain build: one mesh, everything at offset 0.
+struct SingleMesh {
+    static constexpr bool kBatch = false;
+    uint32_t n;
+    __device__ __forceinline__ MeshSpan of_prim(uint32_t) const { return {0u, 0u, n}; }
+};
+
+// Independent meshes laid end to end.  Mesh m owns primitives (and sorted
+// positions, parent slots, cluster slots) [off[m], off[m+1]), BVH2 nodes
+// [2*off[m], 2*off[m] + 2*count - 1) and BVH8 nodes [off8[m], off8[m+1]).
+struct MeshBatch {
+    static constexpr bool kBatch = true;
+    const uint32_t* off;   // meshes + 1 entries
+    const uint32_t* off8;  // meshes + 1 entries, strictly increasing
+    uint32_t meshes;
+    __device__ __forceinline__ MeshSpan span(uint32_t m) const {
+        const uint32_t s = __ldg(off + m);
+        return {m, s, __ldg(off + m + 1) - s};
+    }
+    __device__ __forceinline__ MeshSpan of_prim(uint32_t g) const { return span(owner_of(off, 0, meshes - 1, g)); }
+};
+
 }  // namespace nxb

@@ -36,12 +36,20 @@ namespace {
 constexpr int kThreads = 128;
 constexpr uint32_t kMergeThreshold = 16;  // MERGING_THRESHOLD, BinaryBuilder.cu:10
 
-__device__ __forceinline__ uint64_t delta(const uint32_t* k, uint32_t a, uint32_t b) {
-    return (((uint64_t)__ldg(k + a) << 32) | a) ^ (((uint64_t)__ldg(k + b) << 32) | b);
+// Delta (BinaryBuilder.cu:16-28) of sorted positions a and b of the mesh
+// whose first position is s; the index tie-break uses mesh-local positions.
+__device__ __forceinline__ uint64_t delta(const uint32_t* k, uint32_t a, uint32_t b, uint32_t s) {
+    return (((uint64_t)__ldg(k + a) << 32) | (a - s)) ^ (((uint64_t)__ldg(k + b) << 32) | (b - s));
 }
-__device__ __forceinline__ uint64_t delta(const uint64_t* k, uint32_t a, uint32_t b) {
+__device__ __forceinline__ uint64_t delta(const uint64_t* k, uint32_t a, uint32_t b, uint32_t s) {
     const uint64_t d = __ldg(k + a) ^ __ldg(k + b);
-    return d ? d : (uint64_t)(a ^ b);
+    return d ? d : (uint64_t)((a - s) ^ (b - s));
+}
+// Batched 30-bit keys: mesh << 32 | code, sorted as one key; the delta is
+// the 32-bit one of the code.
+__device__ __forceinline__ uint64_t delta(const MeshKey* k, uint32_t a, uint32_t b, uint32_t s) {
+    const uint32_t ka = (uint32_t)__ldg(&k[a].v), kb = (uint32_t)__ldg(&k[b].v);
+    return (((uint64_t)ka << 32) | (a - s)) ^ (((uint64_t)kb << 32) | (b - s));
 }
 
 template <int R>
@@ -164,9 +172,27 @@ __device__ __forceinline__ void merge_root(const MergeCtx& m, uint32_t& cid, uin
     if (lane == 1) cid = kInvalid;
 }
 
+// The mesh of the owner lane: `all` holds the bases of the concatenated
+// arrays; the context returned addresses this mesh's nodes and counter.
+template <typename Seg>
+__device__ __forceinline__ MergeCtx mesh_ctx(const MergeCtx& all, MeshSpan me, uint32_t owner, uint32_t& start) {
+    if constexpr (Seg::kBatch) {
+        const uint32_t mesh = __shfl_sync(kFullMask, me.m, owner);
+        start = __shfl_sync(kFullMask, me.start, owner);
+        const uint32_t count = __shfl_sync(kFullMask, me.count, owner);
+        return MergeCtx{all.nodes + 2ull * start, all.tok, all.parent_of_last + mesh, count, 2 * count - 1, all.err};
+    } else {
+        start = 0;
+        return all;
+    }
+}
+
+// PlocMerge (BinaryBuilder.cu:200-273, the merge part) for the range of
+// lane `owner`; `start` is the first sorted position of its mesh and m
+// addresses that mesh's nodes.
 template <int R>
-__device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t right, uint32_t split, bool final,
-                                        uint32_t* cluster, const MergeCtx& m) {
+__device__ __forceinline__ void merge_windows(uint32_t owner, uint32_t left, uint32_t right, uint32_t split,
+                                              bool final, uint32_t start, uint32_t* cluster, const MergeCtx& m) {
     const uint32_t lane = lane_id();
     const uint32_t l_start = __shfl_sync(kFullMask, left, owner);
     const uint32_t r_end = __shfl_sync(kFullMask, right, owner) + 1;
@@ -176,7 +202,8 @@ __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t 
     // LoadIndices (BinaryBuilder.cu:42-57) for both children at once: lanes
     // 0-15 read the left window, lanes 16-31 the right one.  A child of at
     // most 16 primitives was never merged, so its ids and tokens are the
-    // original ones (token = position); a larger child was stored compacted.
+    // original ones (token = mesh-local position); a larger child was stored
+    // compacted.
     const uint32_t l_len = mid - l_start, r_len = r_end - mid;
     const uint32_t l_size = min(l_len, kMergeThreshold);
     const uint32_t r_size = min(r_len, kMergeThreshold);
@@ -185,12 +212,12 @@ __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t 
         if (lane < l_size) {
             const uint32_t pos = l_start + lane;
             v = __ldcg(cluster + pos);
-            t = l_len > kMergeThreshold ? __ldcg(m.tok + pos) : pos;
+            t = l_len > kMergeThreshold ? __ldcg(m.tok + pos) : pos - start;
         }
     } else if (lane - 16 < r_size) {
         const uint32_t pos = mid + lane - 16;
         v = __ldcg(cluster + pos);
-        t = r_len > kMergeThreshold ? __ldcg(m.tok + pos) : pos;
+        t = r_len > kMergeThreshold ? __ldcg(m.tok + pos) : pos - start;
     }
     const uint32_t vb = __ballot_sync(kFullMask, v != kInvalid);
     const uint32_t num_left = __popc(vb & 0xFFFFu), num_right = __popc(vb >> 16);
@@ -231,6 +258,19 @@ __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t 
     }
 }
 
+// Out of line: the climb loop stays small and the merge gets the registers.
+template <int R, typename Seg>
+__device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t right, uint32_t split, bool final,
+                                        MeshSpan me, uint32_t* cluster, const MergeCtx& all) {
+    if constexpr (Seg::kBatch) {
+        uint32_t start;
+        const MergeCtx m = mesh_ctx<Seg>(all, me, owner, start);
+        merge_windows<R>(owner, left, right, split, final, start, cluster, m);
+    } else {
+        merge_windows<R>(owner, left, right, split, final, 0u, cluster, all);
+    }
+}
+
 // The climb with lane refill.  Each lane climbs from a leaf as in the
 // reference (FindParentId, exchange on the parent's hand-over slot, merge
 // and continue when second to arrive), but a lane that stops takes the next
@@ -244,14 +284,16 @@ __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t 
 // clusters, and (release) after its merges, before the next exchanges.
 constexpr uint32_t kLeafChunk = 64;
 
-template <typename K, int R>
+template <typename K, int R, typename Seg>
 __global__ __launch_bounds__(kThreads) void hploc_kernel(const K* __restrict__ keys, uint32_t* cluster,
-                                                         uint32_t* parent, Node2* nodes, uint32_t n, uint32_t* tok,
-                                                         uint32_t* parent_of_last, uint32_t* leaf_ctr,
+                                                         uint32_t* parent, Node2* nodes, Seg seg, uint32_t total,
+                                                         uint32_t* tok, uint32_t* parent_of_last, uint32_t* leaf_ctr,
                                                          uint32_t* err) {
     const uint32_t lane = lane_id();
-    MergeCtx m{nodes, tok, parent_of_last, n, 2 * n - 1, err};
+    const MergeCtx all{nodes, tok, parent_of_last, total, 2 * total - 1, err};
     uint32_t left = 0, right = 0, split = 0;
+    // the lane's mesh; a plain build has one, known at compile time
+    MeshSpan me = Seg::kBatch ? MeshSpan{0, 0, 0} : seg.of_prim(0);
     bool active = false;
     uint32_t chunk_next = 0, chunk_end = 0;  // warp-uniform
     bool exhausted = false;                  // warp-uniform
@@ -263,18 +305,19 @@ __global__ __launch_bounds__(kThreads) void hploc_kernel(const K* __restrict__ k
                 uint32_t b = 0;
                 if (lane == 0) b = atomicAdd(leaf_ctr, kLeafChunk);
                 b = __shfl_sync(kFullMask, b, 0);
-                if (b >= n) {
+                if (b >= total) {
                     exhausted = true;
                     break;
                 }
                 chunk_next = b;
-                chunk_end = min(b + kLeafChunk, n);
+                chunk_end = min(b + kLeafChunk, total);
             }
             const uint32_t avail = chunk_end - chunk_next;
             const uint32_t rank = __popc(need & lanemask_lt());
             if (!active && ((need >> lane) & 1u) && rank < avail) {
                 left = right = chunk_next + rank;
                 active = true;
+                if constexpr (Seg::kBatch) me = seg.of_prim(left);
             }
             const uint32_t took = min((uint32_t)__popc(need), avail);
             chunk_next += took;
@@ -284,8 +327,9 @@ __global__ __launch_bounds__(kThreads) void hploc_kernel(const K* __restrict__ k
         bool second = false;
         if (active) {
             uint32_t prev;
-            const bool go_right =
-                left == 0 || (right != n - 1 && delta(keys, right, right + 1) < delta(keys, left - 1, left));
+            const bool go_right = left == me.start ||
+                                  (right != me.start + me.count - 1 &&
+                                   delta(keys, right, right + 1, me.start) < delta(keys, left - 1, left, me.start));
             if (go_right) {
                 prev = atomicExch(parent + right, left);
                 if (prev != kInvalid) {
@@ -303,13 +347,13 @@ __global__ __launch_bounds__(kThreads) void hploc_kernel(const K* __restrict__ k
             active = second;
         }
         const uint32_t size = right - left + 1;
-        const bool final = second && size == n;
+        const bool final = second && size == me.count;
         uint32_t todo = __ballot_sync(kFullMask, second && (size > kMergeThreshold || final));
         if (todo) {
             fence_acq_rel_gpu();  // acquire: the siblings' clusters
             while (todo) {
                 const uint32_t owner = __ffs(todo) - 1;
-                ploc_merge<R>(owner, left, right, split, final, cluster, m);
+                ploc_merge<R, Seg>(owner, left, right, split, final, me, cluster, all);
                 todo &= todo - 1;
             }
             __syncwarp();
@@ -318,25 +362,30 @@ __global__ __launch_bounds__(kThreads) void hploc_kernel(const K* __restrict__ k
     }
 }
 
-template <typename K, int R>
-cudaError_t launch_r(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, uint32_t n, uint32_t* tok,
-                     uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err, cudaStream_t s) {
+template <typename K, int R, typename Seg>
+cudaError_t launch_r(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, Seg seg, uint32_t total,
+                     uint32_t* tok, uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err, uint32_t max_per_sm,
+                     cudaStream_t s) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hploc_kernel<K, R>, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hploc_kernel<K, R, Seg>, kThreads, 0);
+    if (max_per_sm && (uint32_t)per_sm > max_per_sm) per_sm = (int)max_per_sm;
     if (per_sm < 1) per_sm = 1;
-    const uint32_t want = (n + kThreads - 1) / kThreads;
+    const uint32_t want = (total + kThreads - 1) / kThreads;
     const uint32_t grid = std::max(1u, std::min(want, (uint32_t)(device_info().sms * per_sm)));
-    hploc_kernel<K, R><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, n, tok, pol, leaf_ctr, err);
+    hploc_kernel<K, R, Seg><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, seg, total, tok, pol, leaf_ctr,
+                                                      err);
     return cudaGetLastError();
 }
 
-template <typename K>
-cudaError_t launch_t(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, uint32_t n, uint32_t radius,
-                     uint32_t* tok, uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err, cudaStream_t s) {
+template <typename K, typename Seg>
+cudaError_t launch_t(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, Seg seg, uint32_t total,
+                     uint32_t radius, uint32_t* tok, uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err,
+                     uint32_t max_per_sm, cudaStream_t s) {
     switch (radius) {
-        case 4: return launch_r<K, 4>(keys, cluster, parent, nodes, n, tok, pol, leaf_ctr, err, s);
-        case 16: return launch_r<K, 16>(keys, cluster, parent, nodes, n, tok, pol, leaf_ctr, err, s);
-        default: return launch_r<K, 8>(keys, cluster, parent, nodes, n, tok, pol, leaf_ctr, err, s);
+        case 4: return launch_r<K, 4>(keys, cluster, parent, nodes, seg, total, tok, pol, leaf_ctr, err, max_per_sm, s);
+        case 16:
+            return launch_r<K, 16>(keys, cluster, parent, nodes, seg, total, tok, pol, leaf_ctr, err, max_per_sm, s);
+        default: return launch_r<K, 8>(keys, cluster, parent, nodes, seg, total, tok, pol, leaf_ctr, err, max_per_sm, s);
     }
 }
 
@@ -345,11 +394,20 @@ cudaError_t launch_t(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* 
 cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
                          uint32_t n, uint32_t radius, uint32_t* tokens, uint32_t* parent_of_last, uint32_t* leaf_ctr,
                          uint32_t* err, cudaStream_t s) {
+    const SingleMesh seg{n};
     if (key_bytes == 4)
-        return launch_t<uint32_t>((const uint32_t*)keys, cluster_idx, parent, nodes, n, radius, tokens,
-                                  parent_of_last, leaf_ctr, err, s);
-    return launch_t<uint64_t>((const uint64_t*)keys, cluster_idx, parent, nodes, n, radius, tokens, parent_of_last,
-                              leaf_ctr, err, s);
+        return launch_t((const uint32_t*)keys, cluster_idx, parent, nodes, seg, n, radius, tokens, parent_of_last,
+                        leaf_ctr, err, 0u, s);
+    return launch_t((const uint64_t*)keys, cluster_idx, parent, nodes, seg, n, radius, tokens, parent_of_last,
+                    leaf_ctr, err, 0u, s);
+}
+
+cudaError_t launch_hploc_batch(const uint64_t* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
+                               const MeshBatch& batch, uint32_t total, uint32_t radius, uint32_t* tokens,
+                               uint32_t* parent_of_last, uint32_t* leaf_ctr, uint32_t* err, uint32_t ctas_per_sm,
+                               cudaStream_t s) {
+    return launch_t(reinterpret_cast<const MeshKey*>(keys), cluster_idx, parent, nodes, batch, total, radius, tokens,
+                    parent_of_last, leaf_ctr, err, ctas_per_sm, s);
 }
 
 }  // namespace nxb

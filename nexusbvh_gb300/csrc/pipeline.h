@@ -42,7 +42,8 @@ struct SortPlan {
     uint32_t shift[kMaxSortPasses];
     uint32_t bits[kMaxSortPasses];
 };
-SortPlan make_sort_plan(uint32_t begin_bit, uint32_t end_bit);
+// Passes of at most digit_bits (1..8) bits each, lowest digit first.
+SortPlan make_sort_plan(uint32_t begin_bit, uint32_t end_bit, uint32_t digit_bits = kRadixBits);
 
 struct DeviceInfo {
     int sms;
@@ -105,6 +106,84 @@ cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster
 cudaError_t launch_bvh8_init(uint64_t* pairs, uint32_t n, uint32_t* ctr, cudaStream_t s);
 cudaError_t launch_bvh8(const Node2* bvh2, uint32_t n, Node8* out, uint32_t cap, uint32_t* prim_idx, uint64_t* pairs,
                         uint32_t* ctr, uint32_t* err, cudaStream_t s);
+// ---------------------------------------------------------------- batches
+// The same stages over independent meshes laid end to end (MeshBatch in
+// common.cuh): one launch per stage for the whole batch.
+// scene_ord: 6 words per mesh, zero on entry.
+cudaError_t launch_batch_bounds(const void* prims, int prim_type, const MeshBatch& batch, uint32_t total,
+                                Node2* nodes, uint32_t* scene_ord, cudaStream_t s);
+// keys: mesh << 32 | 30-bit code; vals: mesh-local primitive index; hist:
+// kMaxSortPasses x kRadixBins words, zero on entry.
+cudaError_t launch_batch_morton(const Node2* nodes, const MeshBatch& batch, uint32_t total, const uint32_t* scene_ord,
+                                uint64_t* keys, uint32_t* vals, const SortPlan& plan, uint32_t* hist,
+                                const MortonFused& fill, cudaStream_t s);
+// parent_of_last: one word per mesh holding INVALID on entry; ctas_per_sm
+// caps the persistent grid (0: as many CTAs as fit).
+cudaError_t launch_hploc_batch(const uint64_t* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
+                               const MeshBatch& batch, uint32_t total, uint32_t radius, uint32_t* tokens,
+                               uint32_t* parent_of_last, uint32_t* leaf_ctr, uint32_t* err, uint32_t ctas_per_sm,
+                               cudaStream_t s);
+// pairs: `slots` = off8[meshes] uint64 slots; ctr: kBvh8CtrWords words.
+cudaError_t launch_bvh8_batch_init(uint64_t* pairs, uint32_t slots, const MeshBatch& batch, uint32_t* ctr,
+                                   uint32_t* mesh_nodes, uint32_t* mesh_leaves, cudaStream_t s);
+cudaError_t launch_bvh8_batch(const Node2* bvh2, const MeshBatch& batch, uint32_t total, Node8* out, uint32_t slots,
+                              uint32_t* prim_idx, uint64_t* pairs, uint32_t* ctr, uint32_t* mesh_nodes,
+                              uint32_t* mesh_leaves, uint32_t* err, cudaStream_t s);
+cudaError_t launch_batch_finalize(const MeshBatch& batch, const uint32_t* scene_ord, const uint32_t* mesh_nodes,
+                                  const uint32_t* mesh_leaves, nxb_batch_mesh* out, cudaStream_t s);
+// One batched build's device memory (a single allocation carved into
+// 256-byte aligned segments; batch.cu).  off/off8 hold the mesh offsets and
+// the BVH8 offsets; results receives one nxb_batch_mesh per mesh.
+struct BatchCtrl {
+    uint32_t error_word;
+    uint32_t leaf_ctr;
+    uint32_t pad[30];
+    uint32_t tile_ctr[kMaxSortPasses];
+    uint32_t hist[kMaxSortPasses][kRadixBins];
+};
+struct BatchArena {
+    uint32_t meshes = 0, total = 0, slots = 0, mesh_bits = 0;
+    size_t bytes = 0;
+    uint32_t* off = nullptr;
+    uint32_t* off8 = nullptr;
+    unsigned char* zero_begin = nullptr;
+    size_t zero_bytes = 0;
+    BatchCtrl* ctrl = nullptr;
+    uint32_t* scene_ord = nullptr;
+    uint32_t* parent = nullptr;  // then parent_of_last, one word per mesh
+    uint32_t* pol = nullptr;
+    size_t ones_words = 0;
+    uint32_t* lookback = nullptr;
+    size_t lookback_words_per_pass = 0;
+    uint32_t* ctr8 = nullptr;
+    uint32_t* mesh_nodes = nullptr;
+    uint32_t* mesh_leaves = nullptr;
+    uint64_t* keys_a = nullptr;
+    uint64_t* keys_b = nullptr;
+    uint32_t* vals_a = nullptr;
+    uint32_t* vals_b = nullptr;
+    uint64_t* pairs = nullptr;
+    Node2* bvh2 = nullptr;
+    Node8* bvh8 = nullptr;
+    uint32_t* prim_idx = nullptr;
+    nxb_batch_mesh* results = nullptr;
+};
+struct BatchTuning {
+    uint32_t digit_bits = 8, radius = 8, hploc_ctas_per_sm = 0;
+};
+// BVH8 node capacity of one mesh (the reference's ceil((4n-1)/7); 1 for an
+// empty mesh, so that BVH8 offsets are strictly increasing).
+uint32_t batch_bvh8_capacity(uint32_t n);
+// Sizes the arena for meshes with host offsets h_off[0..meshes] and fills
+// h_off8[0..meshes]; returns false if the batch is too large.  The device
+// pointers stay null until batch_bind.
+bool batch_layout(const uint32_t* h_off, uint32_t meshes, uint32_t* h_off8, BatchArena* a);
+void batch_bind(unsigned char* base, BatchArena* a);
+bool batch_digit_ok(uint32_t mesh_bits, uint32_t digit_bits);
+// The batched pipeline on stream s; off/off8 must already be on the device.
+// If h_err is not null, the error word is copied there at the end.
+nxb_status batch_enqueue(const BatchArena& a, const void* prims, nxb_prim_type type, const BatchTuning& t,
+                         uint32_t* h_err, cudaStream_t s);
 // ---------------------------------------------------------------- eval
 cudaError_t launch_bvh2_cost(const Node2* nodes, uint32_t count, const nxb_aabb* root, float* cost, cudaStream_t s);
 cudaError_t launch_bvh8_cost(const Node8* nodes, uint32_t count, const nxb_aabb* root, float* cost, cudaStream_t s);

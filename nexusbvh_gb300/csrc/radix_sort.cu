@@ -263,11 +263,12 @@ cudaError_t run_sort_stall_probe(uint32_t* err_out) {
     return e;
 }
 
-SortPlan make_sort_plan(uint32_t begin_bit, uint32_t end_bit) {
+SortPlan make_sort_plan(uint32_t begin_bit, uint32_t end_bit, uint32_t digit_bits) {
     SortPlan p{};
-    for (uint32_t b = begin_bit; b < end_bit && p.passes < kMaxSortPasses; b += kRadixBits) {
+    digit_bits = std::max(1u, std::min<uint32_t>(digit_bits, kRadixBits));
+    for (uint32_t b = begin_bit; b < end_bit && p.passes < kMaxSortPasses; b += digit_bits) {
         p.shift[p.passes] = b;
-        p.bits[p.passes] = std::min<uint32_t>(kRadixBits, end_bit - b);
+        p.bits[p.passes] = std::min<uint32_t>(digit_bits, end_bit - b);
         p.passes++;
     }
     return p;

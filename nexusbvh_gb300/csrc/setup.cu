@@ -244,6 +244,175 @@ __global__ __launch_bounds__(kThreads) void sort_histogram_kernel(const K* __res
         if (s_hist[i]) atomicAdd(hist + i, s_hist[i]);
 }
 
+// ---------------------------------------------------------------- batches
+// Mesh of element g, searched between the meshes of the warp's first and
+// last elements (usually the same one).
+__device__ __forceinline__ MeshSpan warp_mesh(const MeshBatch& b, uint32_t wfirst, uint32_t wlast, uint32_t g) {
+    const uint32_t lo = owner_of(b.off, 0, b.meshes - 1, wfirst);
+    const uint32_t hi = owner_of(b.off, lo, b.meshes - 1, wlast);
+    return b.span(owner_of(b.off, lo, hi, g));
+}
+
+// Stage 1 over a batch: the same tile staging; mesh m's leaves go to BVH2
+// nodes [2*off[m], 2*off[m] + count) with mesh-local primitive indices, and
+// each mesh's box is reduced per warp into scene_ord[6m .. 6m+5] (a warp
+// that spans two meshes falls back to per-lane atomics).
+template <int FLOATS>
+__global__ __launch_bounds__(kThreads) void batch_bounds_kernel(const float* __restrict__ prims, MeshBatch batch,
+                                                                uint32_t total, Node2* __restrict__ nodes,
+                                                                uint32_t* scene_ord, bool aligned16) {
+    __shared__ __align__(16) float tile[kThreads * FLOATS];
+    const uint32_t tiles = (total + kThreads - 1) / kThreads;
+    for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+        const uint32_t first = t * kThreads;
+        const uint32_t cnt = min((uint32_t)kThreads, total - first);
+        const float* src = prims + (size_t)first * FLOATS;
+        __syncthreads();
+        if (cnt == kThreads && aligned16) {
+            constexpr int V = kThreads * FLOATS / 4;
+            const float4* s4 = reinterpret_cast<const float4*>(src);
+            float4* d4 = reinterpret_cast<float4*>(tile);
+#pragma unroll
+            for (int v = threadIdx.x; v < V; v += kThreads) d4[v] = __ldcs(s4 + v);
+        } else {
+            for (uint32_t v = threadIdx.x; v < cnt * FLOATS; v += kThreads) tile[v] = __ldcs(src + v);
+        }
+        __syncthreads();
+        const uint32_t wfirst = threadIdx.x & ~31u;
+        if (wfirst >= cnt) continue;  // warp-uniform
+        const bool valid = threadIdx.x < cnt;
+        const uint32_t g = first + min(threadIdx.x, cnt - 1);
+        const MeshSpan me = warp_mesh(batch, first + wfirst, first + min(wfirst + 31, cnt - 1), g);
+        Box b;
+        b.mn = make_float3(3.402823466e+38f, 3.402823466e+38f, 3.402823466e+38f);
+        b.mx = make_float3(-3.402823466e+38f, -3.402823466e+38f, -3.402823466e+38f);
+        if (valid) {
+            const float* f = tile + threadIdx.x * FLOATS;
+            if (FLOATS == 9) {
+                float3 v0 = make_float3(f[0], f[1], f[2]);
+                float3 v1 = make_float3(f[3], f[4], f[5]);
+                float3 v2 = make_float3(f[6], f[7], f[8]);
+                b.mn = fmin3(v0, fmin3(v1, v2));
+                b.mx = fmax3(v0, fmax3(v1, v2));
+            } else {
+                b.mn = make_float3(f[0], f[1], f[2]);
+                b.mx = make_float3(f[3], f[4], f[5]);
+            }
+            const uint32_t local = g - me.start;
+            store_node(nodes, 2 * me.start + local, b, kInvalid, local);
+        }
+        const uint32_t m0 = __shfl_sync(kFullMask, me.m, 0);
+        if (__all_sync(kFullMask, !valid || me.m == m0)) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                Box other;
+                other.mn.x = __shfl_down_sync(kFullMask, b.mn.x, o);
+                other.mn.y = __shfl_down_sync(kFullMask, b.mn.y, o);
+                other.mn.z = __shfl_down_sync(kFullMask, b.mn.z, o);
+                other.mx.x = __shfl_down_sync(kFullMask, b.mx.x, o);
+                other.mx.y = __shfl_down_sync(kFullMask, b.mx.y, o);
+                other.mx.z = __shfl_down_sync(kFullMask, b.mx.z, o);
+                grow(b, other);
+            }
+            if (lane_id() == 0) {
+                uint32_t* o = scene_ord + 6ull * m0;
+                atomicMax(o + 0, ~f2ord(b.mn.x));
+                atomicMax(o + 1, ~f2ord(b.mn.y));
+                atomicMax(o + 2, ~f2ord(b.mn.z));
+                atomicMax(o + 3, f2ord(b.mx.x));
+                atomicMax(o + 4, f2ord(b.mx.y));
+                atomicMax(o + 5, f2ord(b.mx.z));
+            }
+        } else if (valid) {
+            uint32_t* o = scene_ord + 6ull * me.m;
+            atomicMax(o + 0, ~f2ord(b.mn.x));
+            atomicMax(o + 1, ~f2ord(b.mn.y));
+            atomicMax(o + 2, ~f2ord(b.mn.z));
+            atomicMax(o + 3, f2ord(b.mx.x));
+            atomicMax(o + 4, f2ord(b.mx.y));
+            atomicMax(o + 5, f2ord(b.mx.z));
+        }
+    }
+}
+
+// Stage 2 over a batch: 30-bit codes from each mesh's own box, written as
+// one sort key mesh << 32 | code, the value being the mesh-local primitive
+// index; digit histograms of every pass of that key fused as in the plain
+// kernel, and the same fill work (parent slots, look-back flags).
+template <bool HIST>
+__global__ __launch_bounds__(kThreads) void batch_morton_kernel(const Node2* __restrict__ nodes, MeshBatch batch,
+                                                                uint32_t total, const uint32_t* scene_ord,
+                                                                uint64_t* __restrict__ keys, uint32_t* vals,
+                                                                uint32_t* hist, MortonArgs a) {
+    __shared__ uint32_t s_hist[HIST ? kMaxSortPasses * kRadixBins : 1];
+    if (HIST)
+        for (int i = threadIdx.x; i < a.pd.passes * kRadixBins; i += kThreads) s_hist[i] = 0;
+    __syncthreads();
+    const uint32_t lane = lane_id();
+    const uint32_t stride = gridDim.x * kThreads;
+    for (uint32_t base = blockIdx.x * kThreads + (threadIdx.x & ~31u); base < total; base += stride) {
+        const uint32_t i = base + lane;
+        const bool valid = i < total;
+        uint64_t key = 0;
+        if (valid) {
+            const MeshSpan me = warp_mesh(batch, base, min(base + 31, total - 1), i);
+            const uint32_t local = i - me.start;
+            const uint32_t* o = scene_ord + 6ull * me.m;
+            const float3 smin = make_float3(ord2f(~__ldg(o + 0)), ord2f(~__ldg(o + 1)), ord2f(~__ldg(o + 2)));
+            const float3 smax = make_float3(ord2f(__ldg(o + 3)), ord2f(__ldg(o + 4)), ord2f(__ldg(o + 5)));
+            const float4* p = reinterpret_cast<const float4*>(nodes + 2ull * me.start + local);
+            float4 lo = __ldcs(p);
+            float2 hi = __ldcs(reinterpret_cast<const float2*>(p + 1));
+            Box b;
+            b.mn = make_float3(lo.x, lo.y, lo.z);
+            b.mx = make_float3(lo.w, hi.x, hi.y);
+            key = ((uint64_t)me.m << 32) | morton_key<uint32_t>(b, smin, smax);
+            keys[i] = key;
+            vals[i] = local;
+        }
+        if (HIST) {
+#pragma unroll 1
+            for (int p = 0; p < a.pd.passes; ++p) {
+                uint32_t d = (uint32_t)(key >> a.pd.shift[p]) & a.pd.mask[p];
+                hist_add(s_hist + p * kRadixBins, d, valid);
+            }
+        }
+    }
+    for (size_t w = (size_t)blockIdx.x * kThreads + threadIdx.x; w < a.zero_vec4; w += stride)
+        a.zero_ptr[w] = make_uint4(0, 0, 0, 0);
+    for (size_t w = (size_t)blockIdx.x * kThreads + threadIdx.x; w < a.ones_vec4; w += stride)
+        a.ones_ptr[w] = make_uint4(kInvalid, kInvalid, kInvalid, kInvalid);
+    if (HIST) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < a.pd.passes * kRadixBins; i += kThreads)
+            if (s_hist[i]) atomicAdd(hist + i, s_hist[i]);
+    }
+}
+
+// Per-mesh results of a batch: scene box, BVH8 range and counts.
+__global__ void batch_finalize_kernel(MeshBatch batch, const uint32_t* scene_ord, const uint32_t* mesh_nodes,
+                                      const uint32_t* mesh_leaves, nxb_batch_mesh* out) {
+    for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < batch.meshes; m += gridDim.x * blockDim.x) {
+        const MeshSpan me = batch.span(m);
+        nxb_batch_mesh r{};
+        if (me.count) {
+            const uint32_t* o = scene_ord + 6ull * m;
+            for (int k = 0; k < 3; ++k) {
+                r.scene_bounds.bmin[k] = ord2f(~o[k]);
+                r.scene_bounds.bmax[k] = ord2f(o[3 + k]);
+            }
+        }
+        r.prim_offset = me.start;
+        r.prim_count = me.count;
+        r.bvh2_offset = 2 * me.start;
+        r.bvh2_node_count = me.count ? 2 * me.count - 1 : 0;
+        r.bvh8_offset = __ldg(batch.off8 + m);
+        r.bvh8_node_count = mesh_nodes[m];
+        r.bvh8_leaf_count = mesh_leaves[m];
+        out[m] = r;
+    }
+}
+
 PassDigits to_digits(const SortPlan& plan) {
     PassDigits pd{};
     pd.passes = plan.passes;
@@ -318,6 +487,38 @@ cudaError_t launch_sort_histogram(uint32_t key_bytes, const void* keys, uint32_t
         sort_histogram_kernel<uint32_t><<<grid, kThreads, 0, s>>>((const uint32_t*)keys, n, pd, hist);
     else
         sort_histogram_kernel<uint64_t><<<grid, kThreads, 0, s>>>((const uint64_t*)keys, n, pd, hist);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_bounds(const void* prims, int prim_type, const MeshBatch& batch, uint32_t total,
+                                Node2* nodes, uint32_t* scene_ord, cudaStream_t s) {
+    bool aligned = (reinterpret_cast<uintptr_t>(prims) & 15u) == 0;
+    uint32_t grid = grid_for(total, 8);
+    if (prim_type == NXB_PRIM_TRIANGLE)
+        batch_bounds_kernel<9><<<grid, kThreads, 0, s>>>((const float*)prims, batch, total, nodes, scene_ord, aligned);
+    else
+        batch_bounds_kernel<6><<<grid, kThreads, 0, s>>>((const float*)prims, batch, total, nodes, scene_ord, aligned);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_morton(const Node2* nodes, const MeshBatch& batch, uint32_t total, const uint32_t* scene_ord,
+                                uint64_t* keys, uint32_t* vals, const SortPlan& plan, uint32_t* hist,
+                                const MortonFused& f, cudaStream_t s) {
+    MortonArgs a{};
+    a.pd = to_digits(plan);
+    a.zero_ptr = reinterpret_cast<uint4*>(f.zero_ptr);
+    a.zero_vec4 = f.zero_words / 4;
+    a.ones_ptr = reinterpret_cast<uint4*>(f.ones_ptr);
+    a.ones_vec4 = f.ones_words / 4;
+    batch_morton_kernel<true><<<grid_for(total, 8), kThreads, 0, s>>>(nodes, batch, total, scene_ord, keys, vals,
+                                                                        hist, a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_finalize(const MeshBatch& batch, const uint32_t* scene_ord, const uint32_t* mesh_nodes,
+                                  const uint32_t* mesh_leaves, nxb_batch_mesh* out, cudaStream_t s) {
+    const uint32_t grid = std::max(1u, std::min<uint32_t>((batch.meshes + 255) / 256, 1024u));
+    batch_finalize_kernel<<<grid, 256, 0, s>>>(batch, scene_ord, mesh_nodes, mesh_leaves, out);
     return cudaGetLastError();
 }
 

@@ -188,6 +188,31 @@ __global__ void bvh8_init_kernel(uint64_t* pairs, uint32_t n, uint32_t* ctr) {
     }
 }
 
+// Batched form: slot m holds the root item of mesh m (empty meshes too,
+// they finish without output); per-mesh node and leaf counters.
+__global__ void bvh8_batch_init_kernel(uint64_t* pairs, uint32_t slots, MeshBatch batch, uint32_t* ctr,
+                                       uint32_t* mesh_nodes, uint32_t* mesh_leaves) {
+    const uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    for (uint32_t i = i0; i < slots; i += gridDim.x * blockDim.x) {
+        uint64_t v = ~0ull;
+        if (i < batch.meshes) {
+            const MeshSpan me = batch.span(i);
+            const uint32_t root = me.count ? 2 * me.count - 2 : 0u;
+            v = ((uint64_t)root << 32) | __ldg(batch.off8 + i);
+            mesh_nodes[i] = me.count ? 1u : 0u;
+            mesh_leaves[i] = 0;
+        }
+        pairs[i] = v;
+    }
+    if (i0 == 0) {
+        ctr[kBvh8Claim] = 0;
+        ctr[kBvh8Nodes] = 0;
+        ctr[kBvh8Leaves] = 0;
+        ctr[kBvh8Alloc] = batch.meshes;
+        ctr[kBvh8Pending] = batch.meshes;
+    }
+}
+
 // Work items are the internal BVH8 nodes only: a parent writes the
 // primitive of each leaf child straight into primIdx (it holds the leaf's
 // node in its slot table), instead of queueing a work item per leaf as the
@@ -197,21 +222,28 @@ __global__ void bvh8_init_kernel(uint64_t* pairs, uint32_t n, uint32_t* ctr) {
 // the next one (warp-aggregated) once its item is done, but only among the
 // slots already allocated, which are ready or about to be; the kernel ends
 // when the count of allocated-but-unfinished items drops to zero.
-__global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict__ b2, uint32_t n, Node8* out,
-                                                        uint32_t cap, uint32_t* prim_idx, uint64_t* pairs,
-                                                        uint32_t* ctr, uint32_t* err) {
+// An item is (mesh-local BVH2 index << 32 | BVH8 index in `out`).  In the
+// batched form (Seg = MeshBatch) the items of all meshes share the queue,
+// the BVH8 index names the mesh, and nodes and leaves are counted per mesh
+// in mesh_nodes / mesh_leaves.
+template <typename Seg>
+__global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict__ b2, Seg seg, Node8* out,
+                                                        uint32_t cap, uint32_t slots, uint32_t* prim_idx,
+                                                        uint64_t* pairs, uint32_t* ctr, uint32_t* mesh_nodes,
+                                                        uint32_t* mesh_leaves, uint32_t* err) {
     extern __shared__ uint32_t s_slots[];
     const SlotTable tab{s_slots};
     const uint32_t lane = lane_id();
-    const uint32_t node_limit = 2 * n - 1;
-    if (n == 1) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            write_node8(out, load_box(b2, 0), LeafZero{b2}, 0, 0, 0xFFFFFFF0u, 0u, 1u);
-            prim_idx[0] = 0;
-            ctr[kBvh8Leaves] = 1;
-            ctr[kBvh8Pending] = 0;
+    if constexpr (!Seg::kBatch) {
+        if (seg.n == 1) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                write_node8(out, load_box(b2, 0), LeafZero{b2}, 0, 0, 0xFFFFFFF0u, 0u, 1u);
+                prim_idx[0] = 0;
+                ctr[kBvh8Leaves] = 1;
+                ctr[kBvh8Pending] = 0;
+            }
+            return;
         }
-        return;
     }
     uint32_t slot = kInvalid;
     bool retired = false;
@@ -238,7 +270,7 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
             const uint32_t rank = __popc(wmask & lanemask_lt());
             if (want && rank < got) {
                 slot = base + rank;
-                if (slot >= n) {
+                if (slot >= slots) {
                     slot = kInvalid;
                     retired = true;
                 }
@@ -263,27 +295,49 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
         }
         idle = 0;
         const uint32_t b2i = (uint32_t)(pr >> 32), b8i = (uint32_t)pr;
+        // the item's mesh: its BVH2 nodes, BVH8 range and primitive range
+        MeshSpan me{0, 0, 0};
+        const Node2* mb2 = b2;
+        uint32_t base8 = 0, cap8 = cap;
         bool internal = false;
         Node2 nd;
         if (ready) {
-            if (b2i >= node_limit || b8i >= cap) {
+            if constexpr (Seg::kBatch) {
+                me = seg.span(owner_of(seg.off8, 0, seg.meshes - 1, b8i));
+                mb2 = b2 + 2ull * me.start;
+                base8 = __ldg(seg.off8 + me.m);
+                cap8 = __ldg(seg.off8 + me.m + 1) - base8;
+            } else {
+                me.count = seg.n;
+            }
+            const uint32_t node_limit = 2 * me.count - 1;
+            if (Seg::kBatch && me.count <= 1) {
+                // an empty mesh has no tree; a one-primitive mesh gets the
+                // single-leaf node (CreateBVH8SingleLeaf, WideConverter.cu:209-222)
+                if (me.count == 1) {
+                    write_node8(out + b8i, load_box(mb2, 0), LeafZero{mb2}, 0, 0, 0xFFFFFFF0u, 0u, 1u);
+                    prim_idx[me.start] = 0;
+                    mesh_leaves[me.m] = 1;
+                }
+            } else if (b2i >= node_limit || b8i - base8 >= cap8) {
                 set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
             } else {
-                nd = load_node(b2, b2i);
+                nd = load_node(mb2, b2i);
                 if (nd.left >= node_limit || nd.right >= node_limit)
                     set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
                 else
                     internal = true;
             }
-            if (!internal) slot = kInvalid;  // reported; the item counts as finished
+            if (!internal) slot = kInvalid;  // done (or reported); the item counts as finished
         }
+        const uint32_t node_limit = 2 * me.count - 1;
         uint32_t inner = 0, count = 0, asg = kInvalid, leaf = 0;
         if (internal) {
             // open BVH2 nodes top-down until 8 children or no inner child
             uint32_t l0 = nd.left, l1 = nd.right;
             uint32_t msb = 0;
             while (true) {
-                const Node2 c0 = load_node(b2, l0), c1 = load_node(b2, l1);
+                const Node2 c0 = load_node(mb2, l0), c1 = load_node(mb2, l1);
                 const bool first = !(half_area(c0.b) < half_area(c1.b));
                 // the smaller-area child takes the re-opened position
                 tab.put(msb, first ? l1 : l0, first ? c1 : c0);
@@ -317,11 +371,12 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
             }
             inner = ninner;
         }
-        // warp-aggregated allocation of inner nodes, leaves and work slots
+        // warp-aggregated allocation of work slots (and, for one mesh, of
+        // BVH8 nodes and leaves; a batch counts those per mesh)
         const uint32_t ic = internal ? (uint32_t)__popc(inner) : 0u;
         const uint32_t lc = internal ? count - ic : 0u;
         const uint32_t wc = ic;  // every inner child becomes a work item of its own
-        const uint32_t packed = ic | (lc << 10) | (wc << 20);
+        const uint32_t packed = Seg::kBatch ? (wc << 20) : (ic | (lc << 10) | (wc << 20));
         uint32_t incl = packed;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -341,22 +396,27 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
         const uint32_t wb = __shfl_sync(kFullMask, bases[2], 31);
         if (internal) {
             const uint32_t excl = incl - packed;
-            const uint32_t child_base = nb + (excl & 0x3FFu);
-            const uint32_t prim_base = lc ? lb + ((excl >> 10) & 0x3FFu) : 0u;
+            uint32_t child_base, prim_base;
+            if constexpr (Seg::kBatch) {
+                child_base = ic ? atomicAdd(mesh_nodes + me.m, ic) : 0u;
+                prim_base = lc ? atomicAdd(mesh_leaves + me.m, lc) : 0u;
+            } else {
+                child_base = nb + (excl & 0x3FFu);
+                prim_base = lc ? lb + ((excl >> 10) & 0x3FFu) : 0u;
+            }
             const uint32_t work_base = wb + (excl >> 20);
-            if (child_base + ic > cap || work_base + wc > n || prim_base + lc > n) {
+            if (child_base + ic > cap8 || work_base + wc > slots || prim_base + lc > me.count) {
                 set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
-                slot = kInvalid;
             } else {
 #pragma unroll
                 for (uint32_t i = 0; i < 8; ++i) {
                     const uint32_t a = nib(asg, i);
                     if ((inner >> i) & 1u) {
                         const uint32_t k = popc_below(inner, i);
-                        const uint64_t pair = ((uint64_t)tab.idx(a) << 32) | (child_base + k);
+                        const uint64_t pair = ((uint64_t)tab.idx(a) << 32) | (base8 + child_base + k);
                         st_relaxed_u64(pairs + work_base + k, pair);
                     } else if ((leaf >> i) & 1u) {
-                        prim_idx[prim_base + popc_below(leaf, i)] = tab.right(a);
+                        prim_idx[me.start + prim_base + popc_below(leaf, i)] = tab.right(a);
                     }
                 }
                 write_node8(out + b8i, nd.b, tab, child_base, prim_base, asg, inner, leaf);
@@ -371,13 +431,23 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
     }
 }
 
-bool g_smem_configured = false;
-
+template <typename Seg>
 cudaError_t configure_smem() {
-    if (g_smem_configured) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(bvh8_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlotSmem);
-    if (!e) g_smem_configured = true;
+    static bool configured = false;
+    if (configured) return cudaSuccess;
+    cudaError_t e =
+        cudaFuncSetAttribute(bvh8_kernel<Seg>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlotSmem);
+    if (!e) configured = true;
     return e;
+}
+
+template <typename Seg>
+uint32_t persistent_grid(uint32_t items) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh8_kernel<Seg>, kThreads, kSlotSmem);
+    if (per_sm < 1) per_sm = 1;
+    const uint32_t want = (items + kThreads - 1) / kThreads;
+    return std::max(1u, std::min(want, (uint32_t)(device_info().sms * per_sm)));
 }
 
 }  // namespace
@@ -388,7 +458,7 @@ cudaError_t run_bvh8_stall_probe(uint32_t* err_out) {
     const uint32_t n = 2;
     unsigned char* buf = nullptr;
     const size_t bytes = 4 * (kBvh8CtrWords + 32) + 3 * sizeof(Node2) + 2 * sizeof(Node8) + 8 * n + 4 * n;
-    cudaError_t e = configure_smem();
+    cudaError_t e = configure_smem<SingleMesh>();
     if (!e) e = cudaMalloc(&buf, bytes);
     if (e) return e;
     uint32_t* ctr = (uint32_t*)buf;  // 256-byte aligned
@@ -405,7 +475,8 @@ cudaError_t run_bvh8_stall_probe(uint32_t* err_out) {
     c[kBvh8Pending] = 1;  // ... but its pair is never written
     if (!e) e = cudaMemcpy(ctr, c, sizeof(c), cudaMemcpyHostToDevice);
     if (!e) {
-        bvh8_kernel<<<1, kThreads, kSlotSmem>>>(b2, n, out, 2, prim, pairs, ctr, err);
+        bvh8_kernel<SingleMesh><<<1, kThreads, kSlotSmem>>>(b2, SingleMesh{n}, out, 2, n, prim, pairs, ctr, nullptr,
+                                                            nullptr, err);
         e = cudaGetLastError();
     }
     if (!e) e = cudaMemcpy(err_out, err, 4, cudaMemcpyDeviceToHost);
@@ -421,14 +492,27 @@ cudaError_t launch_bvh8_init(uint64_t* pairs, uint32_t n, uint32_t* ctr, cudaStr
 
 cudaError_t launch_bvh8(const Node2* bvh2, uint32_t n, Node8* out, uint32_t cap, uint32_t* prim_idx, uint64_t* pairs,
                         uint32_t* ctr, uint32_t* err, cudaStream_t s) {
-    cudaError_t e = configure_smem();
+    cudaError_t e = configure_smem<SingleMesh>();
     if (e) return e;
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh8_kernel, kThreads, kSlotSmem);
-    if (per_sm < 1) per_sm = 1;
-    uint32_t want = (n + kThreads - 1) / kThreads;
-    uint32_t grid = std::max(1u, std::min(want, (uint32_t)(device_info().sms * per_sm)));
-    bvh8_kernel<<<grid, kThreads, kSlotSmem, s>>>(bvh2, n, out, cap, prim_idx, pairs, ctr, err);
+    bvh8_kernel<SingleMesh><<<persistent_grid<SingleMesh>(n), kThreads, kSlotSmem, s>>>(
+        bvh2, SingleMesh{n}, out, cap, n, prim_idx, pairs, ctr, nullptr, nullptr, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bvh8_batch_init(uint64_t* pairs, uint32_t slots, const MeshBatch& batch, uint32_t* ctr,
+                                   uint32_t* mesh_nodes, uint32_t* mesh_leaves, cudaStream_t s) {
+    uint32_t grid = std::max(1u, std::min<uint32_t>((slots + 255) / 256, (uint32_t)device_info().sms * 8));
+    bvh8_batch_init_kernel<<<grid, 256, 0, s>>>(pairs, slots, batch, ctr, mesh_nodes, mesh_leaves);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bvh8_batch(const Node2* bvh2, const MeshBatch& batch, uint32_t total, Node8* out, uint32_t slots,
+                              uint32_t* prim_idx, uint64_t* pairs, uint32_t* ctr, uint32_t* mesh_nodes,
+                              uint32_t* mesh_leaves, uint32_t* err, cudaStream_t s) {
+    cudaError_t e = configure_smem<MeshBatch>();
+    if (e) return e;
+    bvh8_kernel<MeshBatch><<<persistent_grid<MeshBatch>(total), kThreads, kSlotSmem, s>>>(
+        bvh2, batch, out, 0u, slots, prim_idx, pairs, ctr, mesh_nodes, mesh_leaves, err);
     return cudaGetLastError();
 }
 

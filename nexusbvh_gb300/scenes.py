@@ -80,6 +80,33 @@ def clustered(n: int = 12_582_912, seed: int = 2, components: int = 256) -> np.n
     return out
 
 
+def batch_counts(meshes: int = 1024, seed: int = 3, lo: int = 256, hi: int = 262_144) -> np.ndarray:
+    """Primitive counts of a batch: log-uniform in [lo, hi] (1024 meshes,
+    about 38.7M triangles in expectation)."""
+    rng = np.random.default_rng(seed)
+    return np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi + 1), size=meshes))).astype(np.int64).clip(lo, hi)
+
+
+def batch_meshes(counts, seed: int = 3) -> np.ndarray:
+    """Meshes end to end: each a uniform soup (centroids U[0,1]^3, vertex
+    offsets U[-0.005, 0.005]^3) placed in its own box, origin U[-100, 100]^3
+    and per-axis extent log-U[0.1, 10]."""
+    rng = np.random.default_rng(seed + 1000)
+    total = int(np.sum(counts))
+    out = np.empty((total, 9), dtype=np.float32)
+    at = 0
+    for m, n in enumerate(counts):
+        n = int(n)
+        if n == 0:
+            continue
+        origin = rng.uniform(-100.0, 100.0, size=3)
+        extent = np.exp(rng.uniform(np.log(0.1), np.log(10.0), size=3))
+        soup = uniform_soup(n, seed=seed * 100_003 + m).reshape(n, 3, 3).astype(np.float64)
+        out[at:at + n] = (origin + soup * extent).reshape(n, 9).astype(np.float32)
+        at += n
+    return out
+
+
 def to_boxes(tris: np.ndarray) -> np.ndarray:
     """[n, 9] triangles -> [n, 6] boxes (NXB::AABB layout)."""
     v = tris.reshape(-1, 3, 3)

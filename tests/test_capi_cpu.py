@@ -94,3 +94,26 @@ def test_cpp_facade_compiles(tmp_path):
     proc = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", f"-I{ROOT / 'include'}", "-I/usr/local/cuda/include",
                            str(src)], capture_output=True, text=True)
     assert proc.returncode == 0, proc.stderr
+
+
+def test_batch_argument_checks_need_no_device(lib):
+    import numpy as np
+    h = ctypes.c_void_p()
+    c30 = nxb.BuildConfig(prioritize_speed=True).to_c()
+    c63 = nxb.BuildConfig(prioritize_speed=False).to_c()
+    ok = np.array([0, 10, 20], dtype=np.uint32)
+    dec = np.array([0, 10, 5], dtype=np.uint32)
+    first = np.array([3, 10, 20], dtype=np.uint32)
+    assert lib.nxb_batch_create(1, ok.ctypes.data, 2, None, ctypes.byref(h)) == 2      # default = 63-bit
+    assert lib.nxb_batch_create(1, ok.ctypes.data, 2, ctypes.byref(c63), ctypes.byref(h)) == 2
+    assert lib.nxb_batch_create(1, dec.ctypes.data, 2, ctypes.byref(c30), ctypes.byref(h)) == 1
+    assert lib.nxb_batch_create(1, first.ctypes.data, 2, ctypes.byref(c30), ctypes.byref(h)) == 1
+    assert lib.nxb_batch_create(1, ok.ctypes.data, 0, ctypes.byref(c30), ctypes.byref(h)) == 1
+    assert lib.nxb_batch_create(5, ok.ctypes.data, 2, ctypes.byref(c30), ctypes.byref(h)) == 1
+    assert lib.nxb_batch_create(1, None, 2, ctypes.byref(c30), ctypes.byref(h)) == 1
+    bad_r = nxb.BuildConfig(prioritize_speed=True, search_radius=5).to_c()
+    assert lib.nxb_batch_create(1, ok.ctypes.data, 2, ctypes.byref(bad_r), ctypes.byref(h)) == 2
+    big = np.array([0, 1 << 30], dtype=np.uint32)
+    assert lib.nxb_batch_create(1, big.ctypes.data, 1, ctypes.byref(c30), ctypes.byref(h)) == 2
+    assert lib.nxb_batch_destroy(None) == 1
+    assert lib.nxb_batch_build(None, None, None, None) == 1
