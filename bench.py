@@ -53,6 +53,9 @@ WORKLOADS = {
                   "its own box (origin U[-100,100]^3, extent log-U[0.1,10])", 30),
 }
 BATCH_WORKLOADS = {"batch1024": (1024, 3)}
+WORKLOADS["served"] = ("served: Poisson(200/s) requests, n log-U[1024, 4194304] from the soup / sphere / clustered "
+                       "generators with equal probability, every 100th a 28,311,552-triangle clustered build, "
+                       "32 GiB server budget", 30)
 
 # Algorithmic bytes per triangle of each stage (k = key bytes, P = passes):
 # bounds R36+W32; Morton R24 + W k + W4; sort 2P(k+4)+k; H-PLOC k+72;
@@ -479,6 +482,124 @@ def run_batch(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def served_requests(count: int, seed: int = 11):
+    """(kind, n, key_bits) of each request: kind 0 soup, 1 sphere, 2 clustered,
+    3 the 28,311,552-triangle clustered build every 100th request."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        if i % 100 == 99:
+            out.append((3, 28_311_552, 63))
+            continue
+        kind = int(rng.integers(0, 3))
+        n = int(np.exp(rng.uniform(np.log(1024), np.log(4_194_304 + 1))))
+        key_bits = 30 if kind == 0 else (63 if kind == 2 else int(rng.choice([30, 63])))
+        out.append((kind, min(n, 4_194_304), key_bits))
+    return out
+
+
+def run_served(args, world, rank, local):
+    """Served form: a build server (nxb_server_*) fed Poisson arrivals; per
+    request latency = submit -> completion, p50/p99 over the timed requests."""
+    import threading
+    import torch
+    import nexusbvh_gb300 as nxb
+    from nexusbvh_gb300 import scenes
+
+    torch.cuda.set_device(local)
+    nxb.load()
+    pools = [scenes.uniform_soup(4_194_304, seed=0), scenes.displaced_sphere(2048, 1024, seed=1),
+             scenes.clustered(4_194_304, seed=2), scenes.clustered(28_311_552, seed=5)]
+    host = [torch.from_numpy(p).pin_memory() for p in pools]
+    dev = [t.cuda() for t in host]
+    total = args.warmup + args.steps
+    reqs = served_requests(total)
+    rate = 200.0
+    rng = np.random.default_rng(12)
+    gaps = rng.exponential(1.0 / rate, size=total)
+
+    def run_pass(on_device: bool):
+        srv = nxb.Server(budget_bytes=32 << 30)
+        lat, queue, batched = [], [], 0
+        tickets = []
+        done = threading.Event()
+
+        def drain():
+            nonlocal batched
+            for i, t in enumerate(iter(tickets_q.get, None)):
+                r = srv.wait(t)
+                if i >= args.warmup:
+                    lat.append(r.latency_ms)
+                    queue.append(r.queue_ms)
+                    batched += r.batched_with > 1
+                srv.release(t)
+            done.set()
+
+        import queue as _q
+        tickets_q = _q.Queue()
+        th = threading.Thread(target=drain)
+        th.start()
+        t0 = time.perf_counter()
+        at = t0
+        start_timed = None
+        for i, (kind, n, kb) in enumerate(reqs):
+            at += gaps[i]
+            wait = at - time.perf_counter()
+            if wait > 0.0005:
+                time.sleep(wait - 0.0003)  # leave the GIL to the draining thread
+            while time.perf_counter() < at:
+                pass
+            if i == args.warmup:
+                start_timed = time.perf_counter()
+            src = (dev if on_device else host)[kind][:n]
+            cfg = nxb.BuildConfig(prioritize_speed=kb == 30)
+            if on_device:
+                t = srv.submit(src, cfg)
+            else:
+                t = srv.submit(src.numpy(), cfg)
+            tickets.append(t)
+            tickets_q.put(t)
+        tickets_q.put(None)
+        th.join()
+        wall = time.perf_counter() - (start_timed or t0)
+        st = srv.stats()
+        srv.close()
+        tris = sum(n for _, n, _ in reqs[args.warmup:])
+        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "mean_ms": float(np.mean(lat)), "max_ms": float(np.max(lat)),
+                "queue_p99_ms": float(np.percentile(queue, 99)), "requests": len(lat),
+                "batched_requests": batched, "wall_s": wall, "mtris_s": tris / wall / 1e6,
+                "peak_bytes": int(st.peak_bytes_in_use), "builds": int(st.builds),
+                "batched_builds": int(st.batched_builds)}
+
+    with ClockSampler(local) as clocks:
+        resident = run_pass(True)
+        hostin = run_pass(False)
+    if rank != 0:
+        return
+    n_big = sum(1 for k, _, _ in reqs[args.warmup:] if k == 3)
+    line = {
+        "metric": "p99 request latency, served builds (submit -> BVH8 done)",
+        "value": round(resident["p99_ms"], 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(resident["mean_ms"], 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generators standing in for the reference's scene files)",
+        "config": {"workload": WORKLOADS["served"][0], "requests": args.steps, "big_requests": n_big,
+                   "budget_gib": 32, "streams": 4, "batch_max_prims": 65536,
+                   "l2": "each request's input is streamed once; the big builds exceed L2",
+                   "device_resident": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in resident.items()},
+                   "host_input": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in hostin.items()}},
+        "roofline": None,
+        "e2e": {"value": round(hostin["p99_ms"], 3), "unit": "ms",
+                "h2d_bytes_per_step": int(np.mean([n * 36 for _, n, _ in reqs[args.warmup:]])),
+                "d2h_bytes_per_step": 40,
+                "call": "nxb_server_submit with host (pinned) input, nxb_server_wait, nxb_server_release"},
+        "gpu_launches": None,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, world, rank, local):
     """The reference arm.  The reference's path has no CPU implementation,
     and its own CUDA build is not run on the GPU any more: its H-PLOC kernel
@@ -489,6 +610,11 @@ def run_reference(args, world, rank, local):
     algorithm (the oracle port) on all host cores, each step one CPU build
     of a bounded prefix sample of the workload."""
     if rank != 0:
+        return
+    if args.workload == "served":
+        print(json.dumps({"impl": "reference", "unavailable": "the served form (a build server with admission and "
+                          "continuous batching) has no counterpart in the reference, which is a per-mesh library "
+                          "call"}), flush=True)
         return
     import oracle
 
@@ -564,6 +690,8 @@ def main():
             run_reference(args, world, rank, local)
         elif args.workload in BATCH_WORKLOADS:
             run_batch(args, world, rank, local)
+        elif args.workload == "served":
+            run_served(args, world, rank, local)
         else:
             run_ours(args, world, rank, local)
     finally:

@@ -364,6 +364,60 @@ nxb_status nxb_batch_get_tuning(const nxb_batch* batch, nxb_batch_tuning* out_tu
  * nxb_free_host_bvh8) after a successful build. */
 nxb_status nxb_batch_mesh_bvh8_to_host(const nxb_batch* batch, uint32_t mesh, nxb_bvh8* host_bvh);
 
+/* ------------------------------------------------------------- build server */
+/* No counterpart in the reference's API.  A build server for a stream of
+ * independent requests (one mesh each): requests are admitted against a
+ * device-memory budget, started as soon as a stream slot and memory are free
+ * (continuous batching: small requests of the same prim type that wait at
+ * the same time are built together by the batched pipeline, one launch per
+ * stage; large or 63-bit requests run the plain pipeline), and their BVH8s
+ * kept in server memory until released.  A request's result is the one a
+ * plain build of that mesh alone gives (same tree, boxes and quantisation;
+ * only BVH8 node numbering may differ, as between two plain builds).
+ * One worker thread per server drives the GPU; every call is thread-safe. */
+typedef struct nxb_server nxb_server; /* opaque */
+
+typedef struct nxb_server_config {
+    size_t memory_budget_bytes; /* device memory held at once: inputs, scratch, results (0 = 32 GiB) */
+    uint32_t streams;           /* builds in flight at once (0 = 4) */
+    uint32_t batch_max_prims;   /* requests up to this size may share a batched build (0 = 65536; 1 = never) */
+    uint32_t batch_max_meshes;  /* meshes per batched build (0 = 256) */
+    uint32_t flags;             /* reserved, must be 0 */
+} nxb_server_config;
+
+typedef struct nxb_server_result {
+    nxb_bvh8 bvh8;          /* device arrays owned by the server until nxb_server_release */
+    int32_t status;         /* nxb_status of the build */
+    uint32_t batched_with;  /* meshes in the build that produced it (1 = built alone) */
+    double queue_ms;        /* submit -> launch (host clock) */
+    double latency_ms;      /* submit -> completion seen by the server (host clock) */
+} nxb_server_result;
+
+typedef struct nxb_server_stats {
+    /* builds: GPU builds started; batched_builds: those that built more than
+     * one request; batched_requests: the requests those built */
+    uint64_t submitted, completed, rejected, builds, batched_builds, batched_requests;
+    size_t bytes_in_use, peak_bytes_in_use;
+} nxb_server_stats;
+
+nxb_status nxb_server_create(const nxb_server_config* config, nxb_server** out_server);
+/* Waits for the builds in flight, then frees everything (unreleased results too). */
+nxb_status nxb_server_destroy(nxb_server* server);
+/* Queues one build.  prims is a device pointer if prims_on_device is nonzero,
+ * else host memory (pinned for best latency); either way it must stay valid
+ * until the request completes.  config as for nxb_build_bvh8 (may be NULL).
+ * Returns NXB_ERR_ADMISSION if the request alone needs more than the budget. */
+nxb_status nxb_server_submit(nxb_server* server, const void* prims, int prims_on_device,
+                             nxb_prim_type prim_type, uint32_t prim_count,
+                             const nxb_build_config* config, uint64_t* out_ticket);
+/* Blocks until the request completes; fills *out (its status is also returned). */
+nxb_status nxb_server_wait(nxb_server* server, uint64_t ticket, nxb_server_result* out);
+/* Non-blocking: *done = 1 and *out filled if the request has completed. */
+nxb_status nxb_server_poll(nxb_server* server, uint64_t ticket, nxb_server_result* out, int* done);
+/* Frees a completed request's result memory and forgets the ticket. */
+nxb_status nxb_server_release(nxb_server* server, uint64_t ticket);
+nxb_status nxb_server_get_stats(nxb_server* server, nxb_server_stats* out);
+
 /* Library version and the compile flags that define its numerics. */
 const char* nxb_version(void);
 

@@ -101,6 +101,23 @@ class CBatchTuning(ctypes.Structure):
                 ("build_ms", ctypes.c_float)]
 
 
+class CServerConfig(ctypes.Structure):
+    _fields_ = [("memory_budget_bytes", ctypes.c_size_t), ("streams", ctypes.c_uint32),
+                ("batch_max_prims", ctypes.c_uint32), ("batch_max_meshes", ctypes.c_uint32),
+                ("flags", ctypes.c_uint32)]
+
+
+class CServerResult(ctypes.Structure):
+    _fields_ = [("bvh8", CBVH8), ("status", ctypes.c_int32), ("batched_with", ctypes.c_uint32),
+                ("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
+
+
+class CServerStats(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_uint64) for f in ("submitted", "completed", "rejected", "builds", "batched_builds",
+                                               "batched_requests")] + \
+               [("bytes_in_use", ctypes.c_size_t), ("peak_bytes_in_use", ctypes.c_size_t)]
+
+
 assert ctypes.sizeof(CBVH2) == 40 and ctypes.sizeof(CBVH8) == 56 and ctypes.sizeof(CMetrics) == 36
 assert ctypes.sizeof(CBatchMesh) == 52
 NXB_TUNE_RADIUS = 0x1
@@ -145,6 +162,15 @@ _SIG = {
     "nxb_batch_set_tuning": (ctypes.c_int, [_P, ctypes.POINTER(CBatchTuning)]),
     "nxb_batch_get_tuning": (ctypes.c_int, [_P, ctypes.POINTER(CBatchTuning)]),
     "nxb_batch_mesh_bvh8_to_host": (ctypes.c_int, [_P, _U32, ctypes.POINTER(CBVH8)]),
+    "nxb_server_create": (ctypes.c_int, [ctypes.POINTER(CServerConfig), ctypes.POINTER(ctypes.c_void_p)]),
+    "nxb_server_destroy": (ctypes.c_int, [_P]),
+    "nxb_server_submit": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, _U32, _P,
+                                         ctypes.POINTER(ctypes.c_uint64)]),
+    "nxb_server_wait": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.POINTER(CServerResult)]),
+    "nxb_server_poll": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.POINTER(CServerResult),
+                                       ctypes.POINTER(ctypes.c_int)]),
+    "nxb_server_release": (ctypes.c_int, [_P, ctypes.c_uint64]),
+    "nxb_server_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(CServerStats)]),
 }
 
 
@@ -442,6 +468,83 @@ class Batch:
         t = _borrow(a.bvh2_nodes + info.bvh2_offset * 32, nbytes)
         torch.cuda.synchronize()
         return np.frombuffer(t.cpu().numpy().tobytes(), dtype=BVH2_NODE_DTYPE).copy()
+
+
+class Server:
+    """Build server (``nxb_server_*``): continuous batching under a memory budget.
+
+    ``submit`` takes a numpy array (host input, kept alive here until the
+    request completes) or a CUDA tensor (device input) and returns a ticket;
+    ``wait`` returns the ``CServerResult`` whose ``bvh8`` points into server
+    memory until ``release``.
+    """
+
+    def __init__(self, budget_bytes: int = 0, streams: int = 0, batch_max_prims: int = 0, batch_max_meshes: int = 0):
+        self._h = ctypes.c_void_p()
+        c = CServerConfig(budget_bytes, streams, batch_max_prims, batch_max_meshes, 0)
+        check(load().nxb_server_create(ctypes.byref(c), ctypes.byref(self._h)), "nxb_server_create")
+        self._keep = {}
+
+    def close(self) -> None:
+        if self._h:
+            load().nxb_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, prims, config: BuildConfig = BuildConfig()) -> int:
+        t = ctypes.c_uint64()
+        c = config.to_c()
+        if isinstance(prims, np.ndarray):
+            prims = np.ascontiguousarray(prims, dtype=np.float32)
+            ptr, on_dev, n, kind = prims.ctypes.data, 0, prims.shape[0], prims.shape[1]
+        else:
+            ptr, on_dev, n, kind = prims.data_ptr(), 1, int(prims.shape[0]), int(prims.shape[1])
+        ptype = NXB_PRIM_TRIANGLE if kind == 9 else NXB_PRIM_AABB
+        check(load().nxb_server_submit(self._h, ptr, on_dev, ptype, n, ctypes.byref(c), ctypes.byref(t)),
+              "nxb_server_submit")
+        self._keep[t.value] = prims
+        return t.value
+
+    def wait(self, ticket: int) -> CServerResult:
+        r = CServerResult()
+        st = load().nxb_server_wait(self._h, ticket, ctypes.byref(r))
+        self._keep.pop(ticket, None)
+        check(st, "nxb_server_wait")
+        return r
+
+    def poll(self, ticket: int):
+        r = CServerResult()
+        done = ctypes.c_int()
+        check(load().nxb_server_poll(self._h, ticket, ctypes.byref(r), ctypes.byref(done)), "nxb_server_poll")
+        return r if done.value else None
+
+    def release(self, ticket: int) -> None:
+        check(load().nxb_server_release(self._h, ticket), "nxb_server_release")
+
+    def stats(self) -> CServerStats:
+        s = CServerStats()
+        check(load().nxb_server_get_stats(self._h, ctypes.byref(s)), "nxb_server_get_stats")
+        return s
+
+    @staticmethod
+    def bvh8_host(result: CServerResult):
+        """(nodes, prim_idx) numpy copies of a result's BVH8."""
+        lib = load()
+        h = CBVH8()
+        b = result.bvh8
+        check(lib.nxb_bvh8_to_host(ctypes.byref(b), ctypes.byref(h)), "nxb_bvh8_to_host")
+        try:
+            nodes = np.frombuffer(ctypes.string_at(h.nodes, h.node_count * 80), dtype=BVH8_NODE_DTYPE).copy()
+            prim = np.frombuffer(ctypes.string_at(h.prim_idx, h.prim_count * 4), dtype=np.uint32).copy()
+        finally:
+            lib.nxb_free_host_bvh8(ctypes.byref(h))
+        return nodes, prim
 
 
 def selftest_numerics() -> list[int]:

@@ -117,3 +117,18 @@ def test_batch_argument_checks_need_no_device(lib):
     assert lib.nxb_batch_create(1, big.ctypes.data, 1, ctypes.byref(c30), ctypes.byref(h)) == 2
     assert lib.nxb_batch_destroy(None) == 1
     assert lib.nxb_batch_build(None, None, None, None) == 1
+
+
+def test_server_argument_checks_need_no_device(lib):
+    h = ctypes.c_void_p()
+    bad = nxb.CServerConfig(0, 0, 0, 0, 1)
+    assert lib.nxb_server_create(ctypes.byref(bad), ctypes.byref(h)) == 2
+    many = nxb.CServerConfig(0, 65, 0, 0, 0)
+    assert lib.nxb_server_create(ctypes.byref(many), ctypes.byref(h)) == 2
+    assert lib.nxb_server_create(None, None) == 1
+    t = ctypes.c_uint64()
+    assert lib.nxb_server_submit(None, None, 0, 1, 10, None, ctypes.byref(t)) == 1
+    assert lib.nxb_server_wait(None, 1, None) == 1
+    assert lib.nxb_server_release(None, 1) == 1
+    assert lib.nxb_server_destroy(None) == 1
+    assert ctypes.sizeof(nxb.CServerResult) == 80 and ctypes.sizeof(nxb.CServerStats) == 64
