@@ -135,9 +135,15 @@ typedef struct nxb_build_metrics {
 typedef struct nxb_build_config {
     uint32_t prioritize_speed; /* nonzero: 30-bit Morton in 32-bit keys; else 63-bit in 64-bit keys */
     uint32_t search_radius;    /* H-PLOC nearest-neighbour radius: 0 (= 8), 4, 8 or 16 */
-    uint32_t flags;            /* reserved, must be 0 */
+    uint32_t flags;            /* NXB_BUILD_* bits; 0 = the reference's default build */
     uint32_t reserved;
 } nxb_build_config;
+
+/* BVH8 child-slot assignment by the auction algorithm, the reference's
+ * compile-time alternative to the greedy assignment (USE_AUCTION,
+ * NexusBVH/src/Cuda/WideConverter.cu:5,50-102,337-358; off in the reference's
+ * build).  Same tree and boxes, different child order inside BVH8 nodes. */
+#define NXB_BUILD_AUCTION 0x1u
 
 /* -------------------------------------------- reference-shaped entry points */
 /* Builds a BVH2 from n device primitives (nxb_triangle or nxb_aabb).  The
@@ -280,6 +286,13 @@ nxb_status nxb_stage_bvh8(const nxb_bvh2_node* d_bvh2_nodes, uint32_t prim_count
                           nxb_bvh8_node* d_bvh8_nodes, uint32_t* d_prim_idx,
                           uint32_t* d_counts, void* d_scratch, size_t scratch_bytes,
                           uint32_t* d_error_word, struct CUstream_st* stream);
+/* The same with NXB_BUILD_* flags (NXB_BUILD_AUCTION selects the auction
+ * slot assignment). */
+nxb_status nxb_stage_bvh8_ex(const nxb_bvh2_node* d_bvh2_nodes, uint32_t prim_count,
+                             nxb_bvh8_node* d_bvh8_nodes, uint32_t* d_prim_idx,
+                             uint32_t* d_counts, void* d_scratch, size_t scratch_bytes,
+                             uint32_t build_flags, uint32_t* d_error_word,
+                             struct CUstream_st* stream);
 
 /* Cost evaluation (Eval.cu): SAH of a BVH2 (all 2n-1 nodes) and the cost of
  * a BVH8 (children only), relative to the root area; *d_cost is overwritten. */

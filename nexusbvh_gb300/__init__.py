@@ -121,6 +121,7 @@ class CServerStats(ctypes.Structure):
 assert ctypes.sizeof(CBVH2) == 40 and ctypes.sizeof(CBVH8) == 56 and ctypes.sizeof(CMetrics) == 36
 assert ctypes.sizeof(CBatchMesh) == 52
 NXB_TUNE_RADIUS = 0x1
+NXB_BUILD_AUCTION = 0x1
 
 _P = ctypes.c_void_p
 _U32 = ctypes.c_uint32
@@ -148,6 +149,7 @@ _SIG = {
     "nxb_stage_hploc": (ctypes.c_int, [_U32, _P, _P, _P, _U32, _U32, _P, ctypes.c_size_t, _P, _P]),
     "nxb_bvh8_scratch_bytes": (ctypes.c_size_t, [_U32]),
     "nxb_stage_bvh8": (ctypes.c_int, [_P, _U32, _P, _P, _P, _P, ctypes.c_size_t, _P, _P]),
+    "nxb_stage_bvh8_ex": (ctypes.c_int, [_P, _U32, _P, _P, _P, _P, ctypes.c_size_t, _U32, _P, _P]),
     "nxb_eval_bvh2_cost": (ctypes.c_int, [_P, _U32, _P, _P, _P]),
     "nxb_eval_bvh8_cost": (ctypes.c_int, [_P, _U32, _P, _P, _P]),
     "nxb_selftest_numerics": (ctypes.c_int, [_P, _U32]),
@@ -206,12 +208,15 @@ def _stream_ptr(stream=None) -> int:
 
 @dataclasses.dataclass
 class BuildConfig:
-    """NXB::BuildConfig plus the H-PLOC search radius (compile-time in the reference)."""
+    """NXB::BuildConfig plus the H-PLOC search radius and the BVH8 auction
+    assignment (both compile-time in the reference)."""
     prioritize_speed: bool = False
     search_radius: int = 8
+    auction: bool = False
 
     def to_c(self) -> CConfig:
-        return CConfig(1 if self.prioritize_speed else 0, int(self.search_radius), 0, 0)
+        return CConfig(1 if self.prioritize_speed else 0, int(self.search_radius),
+                       NXB_BUILD_AUCTION if self.auction else 0, 0)
 
     @property
     def key_bits(self) -> int:

@@ -159,7 +159,7 @@ nxb_status batch_enqueue(const BatchArena& a, const void* prims, nxb_prim_type t
     NXB_TRY(launch_bvh8_batch_init(a.pairs, a.slots, mb, a.ctr8, a.mesh_nodes, a.mesh_leaves, s));
     if (a.total > 0)
         NXB_TRY(launch_bvh8_batch(a.bvh2, mb, a.total, a.bvh8, a.slots, a.prim_idx, a.pairs, a.ctr8, a.mesh_nodes,
-                                  a.mesh_leaves, &a.ctrl->error_word, s));
+                                  a.mesh_leaves, &a.ctrl->error_word, t.auction, s));
     NXB_TRY(launch_batch_finalize(mb, a.scene_ord, a.mesh_nodes, a.mesh_leaves, a.results, s));
     if (h_err)
         NXB_TRY(cudaMemcpyAsync(h_err, &a.ctrl->error_word, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -172,6 +172,7 @@ using namespace nxb;
 
 struct nxb_batch {
     nxb_prim_type type = NXB_PRIM_TRIANGLE;
+    bool auction = false;
     BatchArena arena;
     nxb_batch_tuning tuning{};
     unsigned char* mem = nullptr;
@@ -190,8 +191,9 @@ nxb_status status_of_word(uint32_t w) {
     return NXB_ERR_DEVICE_INVARIANT;
 }
 
-BatchTuning tuning_of(const nxb_batch_tuning& t) {
+BatchTuning tuning_of(const nxb_batch_tuning& t, bool auction) {
     BatchTuning r;
+    r.auction = auction;
     r.digit_bits = t.sort_digit_bits;
     r.radius = t.search_radius;
     r.hploc_ctas_per_sm = t.hploc_ctas_per_sm;
@@ -201,7 +203,7 @@ BatchTuning tuning_of(const nxb_batch_tuning& t) {
 nxb_status capture(nxb_batch* b, const void* prims) {
     cudaGraph_t g = nullptr;
     NXB_TRY(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeRelaxed));
-    const nxb_status st = batch_enqueue(b->arena, prims, b->type, tuning_of(b->tuning), b->h_err, b->cap_stream);
+    const nxb_status st = batch_enqueue(b->arena, prims, b->type, tuning_of(b->tuning, b->auction), b->h_err, b->cap_stream);
     const cudaError_t ec = cudaStreamEndCapture(b->cap_stream, &g);
     if (st != NXB_OK) {
         if (g) cudaGraphDestroy(g);
@@ -244,7 +246,7 @@ nxb_status nxb_batch_create(nxb_prim_type type, const uint32_t* h_off, uint32_t 
     if (!cfg || !cfg->prioritize_speed) return NXB_ERR_UNSUPPORTED;  // batches sort 30-bit codes
     const uint32_t radius = cfg->search_radius ? cfg->search_radius : 8u;
     if (radius != 4 && radius != 8 && radius != 16) return NXB_ERR_UNSUPPORTED;
-    if (cfg->flags) return NXB_ERR_UNSUPPORTED;
+    if (cfg->flags & ~NXB_BUILD_AUCTION) return NXB_ERR_UNSUPPORTED;
     if (h_off[0] != 0) return NXB_ERR_INVALID_ARGUMENT;
     for (uint32_t m = 0; m < meshes; ++m)
         if (h_off[m + 1] < h_off[m]) return NXB_ERR_INVALID_ARGUMENT;
@@ -256,6 +258,7 @@ nxb_status nxb_batch_create(nxb_prim_type type, const uint32_t* h_off, uint32_t 
         return NXB_ERR_UNSUPPORTED;
     }
     b->type = type;
+    b->auction = (cfg->flags & NXB_BUILD_AUCTION) != 0;
     b->tuning.sort_digit_bits = 8;
     b->tuning.search_radius = radius;
     b->tuning.hploc_ctas_per_sm = 0;

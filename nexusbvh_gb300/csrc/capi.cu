@@ -88,9 +88,11 @@ nxb_status check_config(const nxb_build_config* c) {
     if (!c) return NXB_OK;
     uint32_t r = c->search_radius;
     if (r != 0 && r != 4 && r != 8 && r != 16) return NXB_ERR_UNSUPPORTED;
-    if (c->flags != 0) return NXB_ERR_UNSUPPORTED;
+    if (c->flags & ~NXB_BUILD_AUCTION) return NXB_ERR_UNSUPPORTED;
     return NXB_OK;
 }
+
+bool auction_of(const nxb_build_config* c) { return c && (c->flags & NXB_BUILD_AUCTION); }
 
 nxb_status check_prims(const void* prims, nxb_prim_type t, uint32_t n) {
     if (!prims) return NXB_ERR_INVALID_ARGUMENT;
@@ -153,7 +155,7 @@ nxb_status enqueue_build(const void* prims, nxb_prim_type type, uint32_t n, cons
     if (bvh8) {
         NXB_TRY(launch_bvh8_init(pairs, n, ctrl->bvh8_ctr, s));
         NXB_TRY(launch_bvh8(bvh2, n, bvh8, (uint32_t)bvh8_capacity(n), prim_idx, pairs, ctrl->bvh8_ctr,
-                            &ctrl->error_word, s));
+                            &ctrl->error_word, auction_of(cfg), s));
     }
     NXB_TRY(mark(5));
     if (result) NXB_TRY(launch_finalize(ctrl, result, n, s));
@@ -553,21 +555,30 @@ nxb_status nxb_stage_hploc(uint32_t key_bytes, const void* d_sorted_keys, uint32
 
 size_t nxb_bvh8_scratch_bytes(uint32_t n) { return align_up(8ull * n) + align_up(4 * kBvh8CtrWords); }
 
-nxb_status nxb_stage_bvh8(const nxb_bvh2_node* d_bvh2_nodes, uint32_t n, nxb_bvh8_node* d_bvh8_nodes,
-                          uint32_t* d_prim_idx, uint32_t* d_counts, void* d_scratch, size_t scratch_bytes,
-                          uint32_t* d_error_word, struct CUstream_st* stream) {
+nxb_status nxb_stage_bvh8_ex(const nxb_bvh2_node* d_bvh2_nodes, uint32_t n, nxb_bvh8_node* d_bvh8_nodes,
+                             uint32_t* d_prim_idx, uint32_t* d_counts, void* d_scratch, size_t scratch_bytes,
+                             uint32_t build_flags, uint32_t* d_error_word, struct CUstream_st* stream) {
     if (!d_bvh2_nodes || !d_bvh8_nodes || !d_prim_idx || !d_counts || !d_scratch || n == 0)
         return NXB_ERR_INVALID_ARGUMENT;
     if (n > kMaxPrims) return NXB_ERR_UNSUPPORTED;
+    if (build_flags & ~NXB_BUILD_AUCTION) return NXB_ERR_UNSUPPORTED;
     if (scratch_bytes < nxb_bvh8_scratch_bytes(n)) return NXB_ERR_WORKSPACE_TOO_SMALL;
     uint64_t* pairs = (uint64_t*)d_scratch;
     uint32_t* ctr = reinterpret_cast<uint32_t*>((unsigned char*)d_scratch + align_up(8ull * n));
     NXB_TRY(launch_bvh8_init(pairs, n, ctr, stream));
     NXB_TRY(launch_bvh8(reinterpret_cast<const Node2*>(d_bvh2_nodes), n, reinterpret_cast<Node8*>(d_bvh8_nodes),
-                        (uint32_t)bvh8_capacity(n), d_prim_idx, pairs, ctr, d_error_word, stream));
+                        (uint32_t)bvh8_capacity(n), d_prim_idx, pairs, ctr, d_error_word,
+                        (build_flags & NXB_BUILD_AUCTION) != 0, stream));
     NXB_TRY(cudaMemcpyAsync(d_counts, ctr + kBvh8Nodes, sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
     NXB_TRY(cudaMemcpyAsync(d_counts + 1, ctr + kBvh8Leaves, sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
     return NXB_OK;
+}
+
+nxb_status nxb_stage_bvh8(const nxb_bvh2_node* d_bvh2_nodes, uint32_t n, nxb_bvh8_node* d_bvh8_nodes,
+                          uint32_t* d_prim_idx, uint32_t* d_counts, void* d_scratch, size_t scratch_bytes,
+                          uint32_t* d_error_word, struct CUstream_st* stream) {
+    return nxb_stage_bvh8_ex(d_bvh2_nodes, n, d_bvh8_nodes, d_prim_idx, d_counts, d_scratch, scratch_bytes, 0u,
+                             d_error_word, stream);
 }
 
 nxb_status nxb_eval_bvh2_cost(const nxb_bvh2_node* d_nodes, uint32_t count, const nxb_aabb* d_root, float* d_cost,

@@ -164,6 +164,9 @@ __device__ __forceinline__ Box shfl_box(const Box& b, uint32_t src) {
     return r;
 }
 
+// Asks L2 for the line holding p without waiting for it.
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;

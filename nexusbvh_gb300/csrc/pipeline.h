@@ -104,8 +104,9 @@ cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster
 // pairs: n uint64 slots; ctr: kBvh8CtrWords words (128-byte aligned).
 // Both are initialised by launch_bvh8_init.
 cudaError_t launch_bvh8_init(uint64_t* pairs, uint32_t n, uint32_t* ctr, cudaStream_t s);
+// auction: the reference's USE_AUCTION slot assignment instead of the greedy one.
 cudaError_t launch_bvh8(const Node2* bvh2, uint32_t n, Node8* out, uint32_t cap, uint32_t* prim_idx, uint64_t* pairs,
-                        uint32_t* ctr, uint32_t* err, cudaStream_t s);
+                        uint32_t* ctr, uint32_t* err, bool auction, cudaStream_t s);
 // ---------------------------------------------------------------- batches
 // The same stages over independent meshes laid end to end (MeshBatch in
 // common.cuh): one launch per stage for the whole batch.
@@ -128,7 +129,7 @@ cudaError_t launch_bvh8_batch_init(uint64_t* pairs, uint32_t slots, const MeshBa
                                    uint32_t* mesh_nodes, uint32_t* mesh_leaves, cudaStream_t s);
 cudaError_t launch_bvh8_batch(const Node2* bvh2, const MeshBatch& batch, uint32_t total, Node8* out, uint32_t slots,
                               uint32_t* prim_idx, uint64_t* pairs, uint32_t* ctr, uint32_t* mesh_nodes,
-                              uint32_t* mesh_leaves, uint32_t* err, cudaStream_t s);
+                              uint32_t* mesh_leaves, uint32_t* err, bool auction, cudaStream_t s);
 cudaError_t launch_batch_finalize(const MeshBatch& batch, const uint32_t* scene_ord, const uint32_t* mesh_nodes,
                                   const uint32_t* mesh_leaves, nxb_batch_mesh* out, cudaStream_t s);
 // One batched build's device memory (a single allocation carved into
@@ -170,6 +171,7 @@ struct BatchArena {
 };
 struct BatchTuning {
     uint32_t digit_bits = 8, radius = 8, hploc_ctas_per_sm = 0;
+    bool auction = false;
 };
 // BVH8 node capacity of one mesh (the reference's ceil((4n-1)/7); 1 for an
 // empty mesh, so that BVH8 offsets are strictly increasing).

@@ -206,6 +206,7 @@ nxb_status launch_batch(nxb_server* s, Job* j) {
     if (e) return record_cuda_error(e);
     BatchTuning t;
     t.radius = j->reqs[0]->cfg.search_radius ? j->reqs[0]->cfg.search_radius : 8u;
+    t.auction = (j->reqs[0]->cfg.flags & NXB_BUILD_AUCTION) != 0;
     nxb_status stt = batch_enqueue(a, scratch, type, t, sl->h_err, st);
     if (stt != NXB_OK) return stt;
     // each mesh's BVH8 into its request's own result memory
@@ -303,7 +304,9 @@ Job* pick(nxb_server* s) {
         size_t extra = 0;
         for (auto jt = it; jt != s->queue.end() && take.size() < s->cfg.batch_max_meshes; ++jt) {
             Request* q = *jt;
-            if (!batchable(s, q) || q->type != r->type || q->cfg.search_radius != r->cfg.search_radius) continue;
+            if (!batchable(s, q) || q->type != r->type || q->cfg.search_radius != r->cfg.search_radius ||
+                q->cfg.flags != r->cfg.flags)
+                continue;
             const size_t need = q->scratch_bytes + q->result_bytes;
             if (s->in_use + extra + need > budget) continue;
             if (total + q->n > (1u << 30) - 1) break;
@@ -469,7 +472,7 @@ nxb_status nxb_server_submit(nxb_server* s, const void* prims, int on_device, nx
     if (n > (1u << 30) - 1) return NXB_ERR_UNSUPPORTED;
     if (cfg) {
         const uint32_t r = cfg->search_radius;
-        if ((r != 0 && r != 4 && r != 8 && r != 16) || cfg->flags) return NXB_ERR_UNSUPPORTED;
+        if ((r != 0 && r != 4 && r != 8 && r != 16) || (cfg->flags & ~NXB_BUILD_AUCTION)) return NXB_ERR_UNSUPPORTED;
     }
     auto req = std::make_unique<Request>();
     req->prims = prims;

@@ -34,6 +34,12 @@ namespace {
 constexpr int kThreads = 128;
 constexpr float kQuantStep = 1.0f / 255.0f;  // 1/((1<<NQ)-1), NQ = 8
 constexpr uint32_t kQueueSpinLimit = 1u << 20;
+constexpr uint32_t kFallback = 0xFFFFFFFEu;  // auction_assign: use the greedy assignment
+// Opening a BVH2 node needs its children; the opens of one item form a chain
+// of dependent loads.  With prefetching on, loading a child that is itself
+// internal also asks L2 for that child's two children, so that the next open
+// (or the child's own work item) finds them there.
+constexpr bool kPrefetch = true;
 constexpr int kSlotWords = 9;  // BVH2 index, left, right, box (6 floats)
 constexpr size_t kSlotSmem = (size_t)kThreads * 8 * kSlotWords * sizeof(uint32_t);
 
@@ -115,6 +121,72 @@ __device__ __forceinline__ uint32_t greedy_assign(float3 pc, const Boxes& boxes,
             asg &= ~(0xFu << (4 * slot));
             asg |= c << (4 * slot);
         }
+    }
+    return asg;
+}
+
+// AuctionAssignment (WideConverter.cu:50-102) over the cost table of the
+// reference's USE_AUCTION branch (:337-358): child offsets from the parent
+// centroid scaled so that the parent's largest extent maps to
+// MAX_COST / 2 = 5, prices start at 0, epsilon runs from max(maxCost, 1/n)
+// down to 1/n in steps of 1/THETA = 1/8, bidders are taken last-in first-out
+// from a nibble stack.  The reference's loop has no bound and indexes
+// prices[] with an invalid slot when no reward is finite; here bids are
+// capped and both cases fall back to the greedy assignment.
+constexpr uint32_t kAuctionBidLimit = 4096;
+
+template <typename Boxes>
+__device__ uint32_t auction_assign(const Box& pb, const Boxes& boxes, uint32_t count) {
+    const float max_dim = fmaxf(pb.mx.x - pb.mn.x, fmaxf(pb.mx.y - pb.mn.y, pb.mx.z - pb.mn.z));
+    float cost_scale = max_dim == 0.0f ? 0.0f : 10.0f / max_dim;
+    cost_scale *= 0.5f;
+    const float3 pc = make_float3(pb.mn.x + pb.mx.x, pb.mn.y + pb.mx.y, pb.mn.z + pb.mx.z);
+    float3 off[8];
+    float max_cost = -3.402823466e+38f;
+    for (uint32_t c = 0; c < count; ++c) {
+        const Box cb = boxes.box(c);
+        off[c] = make_float3((pc.x - (cb.mn.x + cb.mx.x)) * cost_scale, (pc.y - (cb.mn.y + cb.mx.y)) * cost_scale,
+                             (pc.z - (cb.mn.z + cb.mx.z)) * cost_scale);
+        const float cost = fabsf(off[c].x) + fabsf(off[c].y) + fabsf(off[c].z);
+        if (cost > max_cost) max_cost = cost;
+    }
+    float prices[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) prices[i] = 0.0f;
+    const float threshold = 1.0f / (float)count;
+    float epsilon = fmaxf(max_cost, threshold);
+    uint32_t asg = kInvalid, bids = 0;
+    while (epsilon >= threshold) {
+        asg = kInvalid;
+        uint32_t bidders = 0x76543210u, waiting = count;
+        while (waiting > 0) {
+            const uint32_t c = nib(bidders, --waiting);
+            float win = -3.402823466e+38f, second = -3.402823466e+38f;
+            uint32_t slot = 0xFu;
+#pragma unroll
+            for (uint32_t s = 0; s < 8; ++s) {
+                const float reward = slot_cost(s, off[c]) - prices[s];
+                if (reward > win) {
+                    second = win;
+                    win = reward;
+                    slot = s;
+                } else if (reward > second) {
+                    second = reward;
+                }
+            }
+            if (slot > 7 || ++bids > kAuctionBidLimit) return kFallback;
+            float bump = (win - second) + epsilon;
+#pragma unroll
+            for (uint32_t s = 0; s < 8; ++s)
+                if (s == slot) prices[s] += bump;
+            const uint32_t prev = nib(asg, slot);
+            asg = (asg & ~(0xFu << (4 * slot))) | (c << (4 * slot));
+            if (prev != 0xFu) {
+                bidders = (bidders & ~(0xFu << (4 * waiting))) | (prev << (4 * waiting));
+                ++waiting;
+            }
+        }
+        epsilon *= 0.125f;
     }
     return asg;
 }
@@ -226,7 +298,7 @@ __global__ void bvh8_batch_init_kernel(uint64_t* pairs, uint32_t slots, MeshBatc
 // batched form (Seg = MeshBatch) the items of all meshes share the queue,
 // the BVH8 index names the mesh, and nodes and leaves are counted per mesh
 // in mesh_nodes / mesh_leaves.
-template <typename Seg>
+template <typename Seg, bool AUCTION>
 __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict__ b2, Seg seg, Node8* out,
                                                         uint32_t cap, uint32_t slots, uint32_t* prim_idx,
                                                         uint64_t* pairs, uint32_t* ctr, uint32_t* mesh_nodes,
@@ -338,6 +410,16 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
             uint32_t msb = 0;
             while (true) {
                 const Node2 c0 = load_node(mb2, l0), c1 = load_node(mb2, l1);
+                if (kPrefetch) {
+                    if (c0.left < node_limit && c0.right < node_limit) {
+                        prefetch_l2(mb2 + c0.left);
+                        prefetch_l2(mb2 + c0.right);
+                    }
+                    if (c1.left < node_limit && c1.right < node_limit) {
+                        prefetch_l2(mb2 + c1.left);
+                        prefetch_l2(mb2 + c1.right);
+                    }
+                }
                 const bool first = !(half_area(c0.b) < half_area(c1.b));
                 // the smaller-area child takes the re-opened position
                 tab.put(msb, first ? l1 : l0, first ? c1 : c0);
@@ -359,7 +441,12 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
                 }
             }
             const float3 pc = make_float3(nd.b.mn.x + nd.b.mx.x, nd.b.mn.y + nd.b.mx.y, nd.b.mn.z + nd.b.mx.z);
-            asg = greedy_assign(pc, tab, count);
+            if constexpr (AUCTION) {
+                asg = auction_assign(nd.b, tab, count);
+                if (asg == kFallback) asg = greedy_assign(pc, tab, count);
+            } else {
+                asg = greedy_assign(pc, tab, count);
+            }
             uint32_t ninner = 0;
 #pragma unroll
             for (uint32_t i = 0; i < 8; ++i) {
@@ -431,23 +518,34 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
     }
 }
 
-template <typename Seg>
+template <typename Seg, bool AUCTION>
 cudaError_t configure_smem() {
     static bool configured = false;
     if (configured) return cudaSuccess;
     cudaError_t e =
-        cudaFuncSetAttribute(bvh8_kernel<Seg>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlotSmem);
+        cudaFuncSetAttribute(bvh8_kernel<Seg, AUCTION>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlotSmem);
     if (!e) configured = true;
     return e;
 }
 
-template <typename Seg>
+template <typename Seg, bool AUCTION>
 uint32_t persistent_grid(uint32_t items) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh8_kernel<Seg>, kThreads, kSlotSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh8_kernel<Seg, AUCTION>, kThreads, kSlotSmem);
     if (per_sm < 1) per_sm = 1;
     const uint32_t want = (items + kThreads - 1) / kThreads;
     return std::max(1u, std::min(want, (uint32_t)(device_info().sms * per_sm)));
+}
+
+template <typename Seg, bool AUCTION>
+cudaError_t launch_wide(const Node2* bvh2, Seg seg, uint32_t items, Node8* out, uint32_t cap, uint32_t slots,
+                        uint32_t* prim_idx, uint64_t* pairs, uint32_t* ctr, uint32_t* mesh_nodes,
+                        uint32_t* mesh_leaves, uint32_t* err, cudaStream_t s) {
+    cudaError_t e = configure_smem<Seg, AUCTION>();
+    if (e) return e;
+    bvh8_kernel<Seg, AUCTION><<<persistent_grid<Seg, AUCTION>(items), kThreads, kSlotSmem, s>>>(
+        bvh2, seg, out, cap, slots, prim_idx, pairs, ctr, mesh_nodes, mesh_leaves, err);
+    return cudaGetLastError();
 }
 
 }  // namespace
@@ -458,7 +556,7 @@ cudaError_t run_bvh8_stall_probe(uint32_t* err_out) {
     const uint32_t n = 2;
     unsigned char* buf = nullptr;
     const size_t bytes = 4 * (kBvh8CtrWords + 32) + 3 * sizeof(Node2) + 2 * sizeof(Node8) + 8 * n + 4 * n;
-    cudaError_t e = configure_smem<SingleMesh>();
+    cudaError_t e = configure_smem<SingleMesh, false>();
     if (!e) e = cudaMalloc(&buf, bytes);
     if (e) return e;
     uint32_t* ctr = (uint32_t*)buf;  // 256-byte aligned
@@ -475,8 +573,8 @@ cudaError_t run_bvh8_stall_probe(uint32_t* err_out) {
     c[kBvh8Pending] = 1;  // ... but its pair is never written
     if (!e) e = cudaMemcpy(ctr, c, sizeof(c), cudaMemcpyHostToDevice);
     if (!e) {
-        bvh8_kernel<SingleMesh><<<1, kThreads, kSlotSmem>>>(b2, SingleMesh{n}, out, 2, n, prim, pairs, ctr, nullptr,
-                                                            nullptr, err);
+        bvh8_kernel<SingleMesh, false><<<1, kThreads, kSlotSmem>>>(b2, SingleMesh{n}, out, 2, n, prim, pairs, ctr,
+                                                                   nullptr, nullptr, err);
         e = cudaGetLastError();
     }
     if (!e) e = cudaMemcpy(err_out, err, 4, cudaMemcpyDeviceToHost);
@@ -491,12 +589,12 @@ cudaError_t launch_bvh8_init(uint64_t* pairs, uint32_t n, uint32_t* ctr, cudaStr
 }
 
 cudaError_t launch_bvh8(const Node2* bvh2, uint32_t n, Node8* out, uint32_t cap, uint32_t* prim_idx, uint64_t* pairs,
-                        uint32_t* ctr, uint32_t* err, cudaStream_t s) {
-    cudaError_t e = configure_smem<SingleMesh>();
-    if (e) return e;
-    bvh8_kernel<SingleMesh><<<persistent_grid<SingleMesh>(n), kThreads, kSlotSmem, s>>>(
-        bvh2, SingleMesh{n}, out, cap, n, prim_idx, pairs, ctr, nullptr, nullptr, err);
-    return cudaGetLastError();
+                        uint32_t* ctr, uint32_t* err, bool auction, cudaStream_t s) {
+    if (auction)
+        return launch_wide<SingleMesh, true>(bvh2, SingleMesh{n}, n, out, cap, n, prim_idx, pairs, ctr, nullptr,
+                                             nullptr, err, s);
+    return launch_wide<SingleMesh, false>(bvh2, SingleMesh{n}, n, out, cap, n, prim_idx, pairs, ctr, nullptr, nullptr,
+                                          err, s);
 }
 
 cudaError_t launch_bvh8_batch_init(uint64_t* pairs, uint32_t slots, const MeshBatch& batch, uint32_t* ctr,
@@ -508,12 +606,12 @@ cudaError_t launch_bvh8_batch_init(uint64_t* pairs, uint32_t slots, const MeshBa
 
 cudaError_t launch_bvh8_batch(const Node2* bvh2, const MeshBatch& batch, uint32_t total, Node8* out, uint32_t slots,
                               uint32_t* prim_idx, uint64_t* pairs, uint32_t* ctr, uint32_t* mesh_nodes,
-                              uint32_t* mesh_leaves, uint32_t* err, cudaStream_t s) {
-    cudaError_t e = configure_smem<MeshBatch>();
-    if (e) return e;
-    bvh8_kernel<MeshBatch><<<persistent_grid<MeshBatch>(total), kThreads, kSlotSmem, s>>>(
-        bvh2, batch, out, 0u, slots, prim_idx, pairs, ctr, mesh_nodes, mesh_leaves, err);
-    return cudaGetLastError();
+                              uint32_t* mesh_leaves, uint32_t* err, bool auction, cudaStream_t s) {
+    if (auction)
+        return launch_wide<MeshBatch, true>(bvh2, batch, total, out, 0u, slots, prim_idx, pairs, ctr, mesh_nodes,
+                                            mesh_leaves, err, s);
+    return launch_wide<MeshBatch, false>(bvh2, batch, total, out, 0u, slots, prim_idx, pairs, ctr, mesh_nodes,
+                                         mesh_leaves, err, s);
 }
 
 }  // namespace nxb

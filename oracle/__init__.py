@@ -48,6 +48,8 @@ def load() -> ctypes.CDLL:
             "orc_stable_sort": (None, [ctypes.c_int, P, U, U, U, P, P]),
             "orc_hploc": (ctypes.c_int, [ctypes.c_int, P, P, U, U, P, P]),
             "orc_bvh8": (ctypes.c_int, [P, U, U, P, U, P, P, P]),
+            "orc_bvh8_ex": (ctypes.c_int, [P, U, U, P, U, P, P, P, U]),
+            "orc_compare_bvh8_unordered": (ctypes.c_uint64, [P, U, P, P, U, P, U, P]),
             "orc_bvh2_cost": (ctypes.c_double, [P, U, P]),
             "orc_bvh8_cost": (ctypes.c_double, [P, U, P]),
             "orc_validate_bvh2": (ctypes.c_uint64, [P, U, U, P]),
@@ -139,15 +141,16 @@ def bvh8_capacity(n: int) -> int:
     return (4 * n - 1 + 6) // 7
 
 
-def bvh8(bvh2_nodes: np.ndarray, n: int, root: int):
-    """-> (nodes NODE8[count], prim_idx uint32[n], error bits)"""
+def bvh8(bvh2_nodes: np.ndarray, n: int, root: int, auction: bool = False):
+    """-> (nodes NODE8[count], prim_idx uint32[n], error bits); auction selects
+    the USE_AUCTION slot assignment (WideConverter.cu:50-102)."""
     cap = bvh8_capacity(n)
     out = np.zeros(cap, dtype=NODE8)
     prim = np.zeros(n, dtype=np.uint32)
     nc = ctypes.c_uint32(0)
     lc = ctypes.c_uint32(0)
-    err = load().orc_bvh8(_p(np.ascontiguousarray(bvh2_nodes)), n, root, _p(out), cap, _p(prim), ctypes.byref(nc),
-                          ctypes.byref(lc))
+    err = load().orc_bvh8_ex(_p(np.ascontiguousarray(bvh2_nodes)), n, root, _p(out), cap, _p(prim),
+                             ctypes.byref(nc), ctypes.byref(lc), 1 if auction else 0)
     return out[: nc.value].copy(), prim, err
 
 
@@ -189,6 +192,16 @@ def compare_bvh8(a: np.ndarray, a_prim: np.ndarray, b: np.ndarray, b_prim: np.nd
     return int(load().orc_compare_bvh8(_p(np.ascontiguousarray(a)), a.shape[0],
                                        _p(np.ascontiguousarray(a_prim, np.uint32)), _p(np.ascontiguousarray(b)),
                                        b.shape[0], _p(np.ascontiguousarray(b_prim, np.uint32)), n))
+
+
+def compare_bvh8_unordered(a: np.ndarray, a_prim: np.ndarray, b: np.ndarray, b_prim: np.ndarray, n: int):
+    """-> (0 if the trees are equal up to the slot order inside nodes, number
+    of node pairs whose slot order differs)"""
+    r = ctypes.c_uint32(0)
+    res = load().orc_compare_bvh8_unordered(_p(np.ascontiguousarray(a)), a.shape[0],
+                                            _p(np.ascontiguousarray(a_prim, np.uint32)), _p(np.ascontiguousarray(b)),
+                                            b.shape[0], _p(np.ascontiguousarray(b_prim, np.uint32)), n, ctypes.byref(r))
+    return int(res), int(r.value)
 
 
 def digest_bvh2(nodes: np.ndarray, root: int, n: int) -> int:

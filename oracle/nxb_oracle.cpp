@@ -601,6 +601,62 @@ uint32_t greedy(const float pc[3], const uint32_t* child, uint32_t n, const Node
     return asg;
 }
 
+// AuctionAssignment (WideConverter.cu:50-102) over the cost table of the
+// USE_AUCTION branch of BuildBVH8Kernel (:337-358).  The two divisions
+// (MAX_COST / maxDim, 1.0f / n) are the fast-math divide on the GPU; they
+// are IEEE divisions here.  Unbounded bidding and a bid with no finite
+// reward (the reference then writes prices[15]) fall back to the greedy
+// assignment, as the GPU kernel does.
+constexpr uint32_t kAuctionBidLimit = 4096;
+
+bool auction(const Box& pb, const uint32_t* child, uint32_t n, const Node2* nodes, uint32_t* out) {
+    float ext[3];
+    for (int a = 0; a < 3; ++a) ext[a] = fsub(pb.mx[a], pb.mn[a]);
+    const float max_dim = fmax_gpu(ext[0], fmax_gpu(ext[1], ext[2]));  // fmaxf(float3), CudaMath.h:1132-1135
+    float cost_scale = max_dim == 0.0f ? 0.0f : ftz(10.0f / max_dim);   // MAX_COST = 10
+    cost_scale = fmul(cost_scale, 0.5f);
+    float pc[3], off[8][3];
+    for (int a = 0; a < 3; ++a) pc[a] = fadd(pb.mn[a], pb.mx[a]);
+    float max_cost = -3.402823466e+38f;
+    for (uint32_t c = 0; c < n; ++c) {
+        const Box& b = nodes[child[c]].b;
+        for (int a = 0; a < 3; ++a) off[c][a] = fmul(fsub(pc[a], fadd(b.mn[a], b.mx[a])), cost_scale);
+        const float cost = fadd(fadd(std::fabs(off[c][0]), std::fabs(off[c][1])), std::fabs(off[c][2]));
+        if (cost > max_cost) max_cost = cost;
+    }
+    float prices[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const float threshold = ftz(1.0f / (float)n);
+    float epsilon = fmax_gpu(max_cost, threshold);
+    uint32_t asg = kInvalid, bids = 0;
+    while (epsilon >= threshold) {
+        asg = kInvalid;
+        uint32_t bidders = 0x76543210u, waiting = n;
+        while (waiting > 0) {
+            const uint32_t c = nib(bidders, --waiting);
+            float win = -3.402823466e+38f, second = -3.402823466e+38f;
+            uint32_t slot = 0xF;
+            for (uint32_t s = 0; s < 8; ++s) {
+                const float reward = fsub(slot_cost(s, off[c]), prices[s]);
+                if (reward > win) {
+                    second = win;
+                    win = reward;
+                    slot = s;
+                } else if (reward > second) {
+                    second = reward;
+                }
+            }
+            if (slot > 7 || ++bids > kAuctionBidLimit) return false;
+            prices[slot] = fadd(prices[slot], fadd(fsub(win, second), epsilon));
+            const uint32_t prev = nib(asg, slot);
+            set_nib(asg, slot, c);
+            if (prev != 0xF) set_nib(bidders, waiting++, prev);
+        }
+        epsilon = fmul(epsilon, 0.125f);  // invTheta, THETA = 8
+    }
+    *out = asg;
+    return true;
+}
+
 // CreateBVH8Node (WideConverter.cu:156-206).  Empty slots keep zero
 // quantised bytes (the reference leaves them unspecified).
 Node8 make_node8(const Box& bounds, const uint32_t* child, uint32_t child_base, uint32_t prim_base, uint32_t asg,
@@ -638,7 +694,7 @@ Node8 make_node8(const Box& bounds, const uint32_t* child, uint32_t child_base, 
 // BuildBVH8Kernel (WideConverter.cu:225-414), with the work slots processed
 // in increasing order (every slot is written by a parent in a lower slot).
 int bvh8(const Node2* nodes, uint32_t n, uint32_t root, Node8* out, uint32_t cap, uint32_t* prim_idx,
-         uint32_t* node_count, uint32_t* leaf_count) {
+         uint32_t* node_count, uint32_t* leaf_count, bool use_auction = false) {
     if (n == 1) {  // CreateBVH8SingleLeaf (WideConverter.cu:209-222)
         uint32_t child[8] = {0};
         out[0] = make_node8(nodes[0].b, child, 0, 0, 0xFFFFFFF0u, 0, 1, nodes);
@@ -685,7 +741,8 @@ int bvh8(const Node2* nodes, uint32_t n, uint32_t root, Node8* out, uint32_t cap
             }
             float pc[3];
             for (int a = 0; a < 3; ++a) pc[a] = fadd(nd.b.mn[a], nd.b.mx[a]);
-            uint32_t asg = greedy(pc, child, count, nodes);
+            uint32_t asg = 0;
+            if (!use_auction || !auction(nd.b, child, count, nodes, &asg)) asg = greedy(pc, child, count, nodes);
             uint32_t new_inner = 0, leaf = 0;
             for (uint32_t i = 0; i < 8; ++i) {
                 if (nib(asg, i) == 0xF) continue;
@@ -856,6 +913,12 @@ int orc_hploc(int key_bytes, const void* sorted_keys, const uint32_t* perm, uint
 int orc_bvh8(const void* bvh2_nodes, uint32_t n, uint32_t root, void* bvh8_nodes, uint32_t cap, uint32_t* prim_idx,
              uint32_t* node_count, uint32_t* leaf_count) {
     return bvh8((const Node2*)bvh2_nodes, n, root, (Node8*)bvh8_nodes, cap, prim_idx, node_count, leaf_count);
+}
+// flags: 1 = auction slot assignment (NXB_BUILD_AUCTION).
+int orc_bvh8_ex(const void* bvh2_nodes, uint32_t n, uint32_t root, void* bvh8_nodes, uint32_t cap,
+                uint32_t* prim_idx, uint32_t* node_count, uint32_t* leaf_count, uint32_t flags) {
+    return bvh8((const Node2*)bvh2_nodes, n, root, (Node8*)bvh8_nodes, cap, prim_idx, node_count, leaf_count,
+                (flags & 1u) != 0);
 }
 
 double orc_bvh2_cost(const void* nodes, uint32_t count, const float* root6) {
@@ -1085,6 +1148,99 @@ uint64_t orc_compare_bvh8(const void* a_v, uint32_t a_count, const uint32_t* a_p
         }
     }
     return pos == a_count ? 0 : pos + 1;
+}
+
+// Order-insensitive comparison of two BVH8s: the same nodes (origin,
+// exponents) with the same children (quantised boxes, primitives, subtrees)
+// in any slot order.  *reordered receives the number of node pairs whose
+// slot order differs.  Used where two slot assignments may legitimately
+// differ on near-ties (the auction assignment evaluated with the GPU's
+// fast-math divide against this file's IEEE divide).
+static uint64_t mix64(uint64_t h, uint64_t v) {
+    h ^= v + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+    return h * 1099511628211ull;
+}
+static bool unordered_hashes(const Node8* nodes, uint32_t count, const uint32_t* prim, uint32_t n,
+                             std::vector<uint64_t>& node_h, std::vector<uint64_t>& child_h) {
+    // child_h[8*i + s]: hash of slot s of node i (0 for an empty slot)
+    node_h.assign(count, 0);
+    child_h.assign(8ull * count, 0);
+    std::vector<std::pair<uint32_t, bool>> stack = {{0, false}};
+    while (!stack.empty()) {
+        auto [i, expanded] = stack.back();
+        stack.pop_back();
+        if (i >= count) return false;
+        const Node8& x = nodes[i];
+        if (!expanded) {
+            stack.push_back({i, true});
+            for (uint32_t s = 0; s < 8; ++s)
+                if (x.meta[s] && ((x.imask >> s) & 1u)) stack.push_back({x.child_base + below(x.imask, s), false});
+            continue;
+        }
+        std::vector<uint64_t> kids;
+        for (uint32_t s = 0; s < 8; ++s) {
+            if (!x.meta[s]) continue;
+            uint64_t h = 1469598103934665603ull;
+            for (int ax = 0; ax < 3; ++ax) h = mix64(h, ((uint64_t)x.qlo[ax][s] << 8) | x.qhi[ax][s]);
+            if ((x.imask >> s) & 1u) {
+                const uint32_t c = x.child_base + below(x.imask, s);
+                if (c >= count) return false;
+                h = mix64(h, node_h[c]);
+            } else {
+                const uint32_t li = x.prim_base + (x.meta[s] & 0x1Fu);
+                if (li >= n) return false;
+                h = mix64(h, 0x1000000000ull | prim[li]);
+            }
+            child_h[8ull * i + s] = h;
+            kids.push_back(h);
+        }
+        std::sort(kids.begin(), kids.end());
+        uint64_t h = 1469598103934665603ull;
+        uint32_t pe[4];
+        std::memcpy(pe, x.p, 12);
+        std::memcpy(&pe[3], x.e, 3);
+        pe[3] &= 0xFFFFFFu;
+        for (int k = 0; k < 4; ++k) h = mix64(h, pe[k]);
+        for (uint64_t k : kids) h = mix64(h, k);
+        node_h[i] = h;
+    }
+    return true;
+}
+
+uint64_t orc_compare_bvh8_unordered(const void* a_v, uint32_t a_count, const uint32_t* a_prim, const void* b_v,
+                                    uint32_t b_count, const uint32_t* b_prim, uint32_t n, uint32_t* reordered) {
+    const Node8* a = (const Node8*)a_v;
+    const Node8* b = (const Node8*)b_v;
+    *reordered = 0;
+    if (a_count != b_count || a_count == 0) return ~0ull;
+    std::vector<uint64_t> ha, ca, hb, cb;
+    if (!unordered_hashes(a, a_count, a_prim, n, ha, ca) || !unordered_hashes(b, b_count, b_prim, n, hb, cb))
+        return ~0ull;
+    if (ha[0] != hb[0]) return 1;
+    // count the node pairs whose slot order differs (walk matched children)
+    std::vector<std::pair<uint32_t, uint32_t>> stack = {{0, 0}};
+    uint32_t visited = 0;
+    while (!stack.empty()) {
+        auto [ia, ib] = stack.back();
+        stack.pop_back();
+        ++visited;
+        bool same = true;
+        for (uint32_t s = 0; s < 8; ++s) same &= ca[8ull * ia + s] == cb[8ull * ib + s];
+        if (!same) ++*reordered;
+        std::vector<std::pair<uint64_t, uint32_t>> xa, xb;
+        for (uint32_t s = 0; s < 8; ++s) {
+            if (a[ia].meta[s] && ((a[ia].imask >> s) & 1u)) xa.push_back({ca[8ull * ia + s], a[ia].child_base + below(a[ia].imask, s)});
+            if (b[ib].meta[s] && ((b[ib].imask >> s) & 1u)) xb.push_back({cb[8ull * ib + s], b[ib].child_base + below(b[ib].imask, s)});
+        }
+        std::sort(xa.begin(), xa.end());
+        std::sort(xb.begin(), xb.end());
+        if (xa.size() != xb.size()) return 2;
+        for (size_t k = 0; k < xa.size(); ++k) {
+            if (xa[k].first != xb[k].first) return 2;
+            stack.push_back({xa[k].second, xb[k].second});
+        }
+    }
+    return visited == a_count ? 0 : 3;
 }
 
 // FNV-1a digests of the canonical DFS serialisations used by

@@ -92,7 +92,7 @@ def stage_hploc(d_sorted_keys, d_perm, d_nodes, n: int, key_bits: int, radius: i
     return nodes
 
 
-def stage_bvh8(d_bvh2_nodes, n: int):
+def stage_bvh8(d_bvh2_nodes, n: int, flags: int = 0):
     t = torch()
     lib = nxb.load()
     cap = (4 * n - 1 + 6) // 7
@@ -102,8 +102,9 @@ def stage_bvh8(d_bvh2_nodes, n: int):
     scratch = lib.nxb_bvh8_scratch_bytes(n)
     d_scr = t.empty(scratch, dtype=t.uint8, device="cuda")
     d_err = t.zeros(1, dtype=t.int32, device="cuda")
-    check(lib.nxb_stage_bvh8(d_bvh2_nodes.data_ptr(), n, d_out.data_ptr(), d_prim.data_ptr(), d_counts.data_ptr(),
-                             d_scr.data_ptr(), scratch, d_err.data_ptr(), stream()), "nxb_stage_bvh8")
+    check(lib.nxb_stage_bvh8_ex(d_bvh2_nodes.data_ptr(), n, d_out.data_ptr(), d_prim.data_ptr(),
+                                d_counts.data_ptr(), d_scr.data_ptr(), scratch, flags, d_err.data_ptr(), stream()),
+          "nxb_stage_bvh8_ex")
     t.cuda.synchronize()
     assert int(d_err.item()) == 0, f"bvh8 error word {int(d_err.item()):#x}"
     counts = host(d_counts).astype(np.uint32)

@@ -222,3 +222,41 @@ def test_errors_are_status_codes(gpu):
     assert lib.nxb_build_bvh8(None, 1, 10, ctypes.byref(c), None, ctypes.byref(out), None) == 1
     assert lib.nxb_build_bvh8(prims.data_ptr(), 1, 0, ctypes.byref(c), None, ctypes.byref(out), None) == 1
     assert lib.nxb_build_bvh8(prims.data_ptr(), 3, 10, ctypes.byref(c), None, ctypes.byref(out), None) == 1
+
+
+@pytest.mark.parametrize("name,make,key_bits", [
+    ("clustered60k-63", lambda: scenes.clustered(60_000, seed=21), 63),
+    ("soup40k-30", lambda: scenes.uniform_soup(40_000, seed=22), 30),
+    ("sphere32k-63", lambda: scenes.displaced_sphere(128, 128, seed=23), 63),
+])
+def test_auction_assignment(gpu, orc, name, make, key_bits):
+    """NXB_BUILD_AUCTION (the reference's USE_AUCTION branch): the BVH8
+    kernel's auction against the oracle's, over the same GPU BVH2.
+
+    Tolerance: the auction scales its cost table by MAX_COST / maxDim and
+    stops at epsilon < 1/n, two divisions that are the fast-math divide on
+    the GPU (as in the reference) and IEEE in the oracle; the auction's bids
+    end in near-ties, so a one-ulp difference can swap two children's slots.
+    The trees must be identical up to slot order inside nodes (same nodes,
+    boxes, quantisation, primitives), with at most 2 % of the nodes in
+    another slot order."""
+    prims = make()
+    n = prims.shape[0]
+    chain = run_chain(prims, key_bits, orc)
+    d_b2 = S.dev(chain["b2"].view(np.uint8))
+    b8_g, prim_g, nc, lc = S.stage_bvh8(d_b2, n, flags=nxb.NXB_BUILD_AUCTION)
+    b8_o, prim_o, err = orc.bvh8(chain["b2"], n, 2 * n - 2, auction=True)
+    assert err == 0 and lc == n and nc == b8_o.shape[0]
+    res, reordered = orc.compare_bvh8_unordered(b8_g, prim_g, b8_o, prim_o, n)
+    assert res == 0, "auction BVH8 differs from the oracle beyond slot order"
+    assert reordered <= 0.02 * nc, f"{reordered} of {nc} nodes in another slot order than the oracle's"
+    errs, rep = orc.validate_bvh8(b8_g, prim_g, n, chain["leaves"])
+    assert errs == 0, rep
+    # the same tree as the greedy build, children in another order
+    assert orc.compare_bvh8(b8_g, prim_g, chain["b8"], chain["prim"], n) != 0
+    rb = S.root_box(chain["b2"], 2 * n - 2)
+    assert abs(orc.bvh8_cost(b8_g, rb) - chain["costs"][1]) <= 1e-3 * chain["costs"][1]
+    # whole pipeline with the flag: the same as the stage call, slot for slot
+    out = nxb.Builder().build(S.dev(prims), nxb.BuildConfig(prioritize_speed=key_bits == 30, auction=True))
+    b8p = S.host(out.nodes.reshape(-1)).view(nxb.BVH8_NODE_DTYPE)
+    assert orc.compare_bvh8(b8p, S.host(out.prim_idx).view(np.uint32), b8_g, prim_g, n) == 0

@@ -198,3 +198,25 @@ def test_fast_math_helpers(orc):
     assert lib.orc_fmin(tiny, np.float32(1.0)) == 0.0
     assert lib.orc_f2u8(300.0) in (44, 255)
     assert lib.orc_f2u8(-3.0) == 0
+
+
+def test_auction_oracle_keeps_the_tree(orc):
+    """The auction assignment only permutes children inside BVH8 nodes: same
+    node count, same cost, valid conservative quantisation."""
+    from nexusbvh_gb300 import scenes
+    p = scenes.clustered(8000, seed=31)
+    o = orc.build(p, 63)
+    g8, gp, ge = orc.bvh8(o["bvh2"], 8000, o["root"])
+    a8, ap, ae = orc.bvh8(o["bvh2"], 8000, o["root"], auction=True)
+    assert ge == 0 and ae == 0 and g8.shape == a8.shape
+    rb = np.concatenate([o["bvh2"][o["root"]]["bmin"], o["bvh2"][o["root"]]["bmax"]]).astype(np.float32)
+    assert abs(orc.bvh8_cost(a8, rb) - orc.bvh8_cost(g8, rb)) <= 1e-6 * orc.bvh8_cost(g8, rb)
+    errs, rep = orc.validate_bvh8(a8, ap, 8000, o["bvh2"][:8000])
+    assert errs == 0, rep
+    assert orc.compare_bvh8(a8, ap, g8, gp, 8000) != 0
+    res, reordered = orc.compare_bvh8_unordered(a8, ap, g8, gp, 8000)
+    assert res == 0 and 0 < reordered <= a8.shape[0]
+    bad = a8.copy()
+    occupied = np.nonzero(bad[0]["meta"])[0][0]
+    bad[0]["qhi"][1][occupied] ^= 1
+    assert orc.compare_bvh8_unordered(bad, ap, g8, gp, 8000)[0] != 0
