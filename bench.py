@@ -73,6 +73,11 @@ def algorithmic_bytes(stage: str, k: int, passes: int, bvh8_nodes_per_tri: float
     }[stage]
 
 
+def _num(x: float, digits: int = 2):
+    """Rounded float for the JSON line; None for a value that was not measured."""
+    return None if x != x else round(x, digits)
+
+
 def peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -349,7 +354,7 @@ def run_batch(args, world, rank, local):
     sptr = int(stream.cuda_stream)
     batch = nxb.Batch(counts, config=nxb.BuildConfig(prioritize_speed=True, search_radius=args.radius))
     t_tune = time.perf_counter()
-    tuning = batch.autotune(d_prims, repeats=2)
+    tuning = batch.tuning() if args.no_autotune else batch.autotune(d_prims, repeats=2)
     t_tune = time.perf_counter() - t_tune
     for _ in range(args.warmup):
         batch.build_async(d_prims)
@@ -420,19 +425,21 @@ def run_batch(args, world, rank, local):
                                           b2.data_ptr(), b8.data_ptr(), pidx.data_ptr(), rbuf.data_ptr(), sptr),
                       "nxb_build_async")
 
-    loop_plain()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    loop_plain()
-    torch.cuda.synchronize()
-    t_loop = time.perf_counter() - t0
-    loop_async()
-    torch.cuda.synchronize()
-    start.record(stream)
-    loop_async()
-    stop.record(stream)
-    torch.cuda.synchronize()
-    t_loop_async = start.elapsed_time(stop) / 1e3
+    t_loop = t_loop_async = float("nan")
+    if not args.no_loop_baseline:
+        loop_plain()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        loop_plain()
+        torch.cuda.synchronize()
+        t_loop = time.perf_counter() - t0
+        loop_async()
+        torch.cuda.synchronize()
+        start.record(stream)
+        loop_async()
+        stop.record(stream)
+        torch.cuda.synchronize()
+        t_loop_async = start.elapsed_time(stop) / 1e3
     if rank != 0:
         return
     pk = peaks()
@@ -457,11 +464,11 @@ def run_batch(args, world, rank, local):
                        "hploc_ctas_per_sm": int(tuning.hploc_ctas_per_sm),
                        "candidates": int(tuning.candidates_tried), "tune_s": round(t_tune, 2)},
             "bvh8_nodes": int(n8),
-            "loop_plain_api_ms": round(t_loop * 1e3, 2),
-            "loop_plain_api_mtris_s": round(n / t_loop / 1e6, 2),
-            "loop_async_ms": round(t_loop_async * 1e3, 2),
-            "speedup_vs_loop_plain_api": round(t_loop * 1e3 / ms, 2),
-            "speedup_vs_loop_async": round(t_loop_async * 1e3 / ms, 2),
+            "loop_plain_api_ms": _num(t_loop * 1e3),
+            "loop_plain_api_mtris_s": _num(n / t_loop / 1e6),
+            "loop_async_ms": _num(t_loop_async * 1e3),
+            "speedup_vs_loop_plain_api": _num(t_loop * 1e3 / ms),
+            "speedup_vs_loop_async": _num(t_loop_async * 1e3 / ms),
         },
         "roofline": {"kernel": "whole batched pipeline", "bound": "hbm", "achieved": round(gbs, 1),
                      "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(gbs / pk["hbm_gbs"], 3), "traffic": None,
@@ -712,6 +719,10 @@ def main():
     ap.add_argument("--radius", type=int, choices=[4, 8, 16], default=8)
     ap.add_argument("--cpu-sample", type=int, default=2_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-loop-baseline", action="store_true",
+                    help="batched workloads: leave out the loop-of-plain-builds comparison")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batched workloads: build with the default tuning instead of tuning first")
     args = ap.parse_args()
     if args.key_bits is None:
         args.key_bits = WORKLOADS[args.workload][1]
