@@ -13,6 +13,9 @@ struct BuildConfig {
     bool prioritizeSpeed = false;
     // H-PLOC search radius (4, 8 or 16); the reference fixes it at 8
     uint32_t searchRadius = 8;
+    // BVH8 child slots by the auction algorithm (the reference's compile-time
+    // USE_AUCTION) instead of the greedy assignment
+    bool useAuction = false;
 };
 
 }  // namespace NXB

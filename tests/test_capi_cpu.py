@@ -90,7 +90,22 @@ def test_cpp_facade_compiles(tmp_path):
         "  NXB::BVHBuildMetrics m;\n"
         "  return NXB::BuildBVH8<NXB::Triangle>(t, n, c, &m);\n"
         "}\n"
-        "NXB::BVH2 g(NXB::AABB* b, uint32_t n) { return NXB::BuildBVH2(b, n); }\n")
+        "NXB::BVH2 g(NXB::AABB* b, uint32_t n) { return NXB::BuildBVH2(b, n); }\n"
+        '#include "NXB/BatchBuilder.h"\n'
+        "NXB::BVH8 h(NXB::Triangle* t, const std::vector<uint32_t>& counts) {\n"
+        "  NXB::BuildConfig c; c.prioritizeSpeed = true; c.useAuction = true;\n"
+        "  NXB::BatchBuilder<NXB::Triangle> b(counts, c);\n"
+        "  b.Autotune(t); b.Build(t);\n"
+        "  return b.MeshBVH8(0);\n"
+        "}\n"
+        "NXB::BVH8 s(const NXB::Triangle* t, uint32_t n) {\n"
+        "  NXB::BuildServer srv(1ull << 30, 2);\n"
+        "  uint64_t k = srv.Submit(t, n, false);\n"
+        "  nxb_server_result info{};\n"
+        "  NXB::BVH8 r = srv.Wait(k, &info);\n"
+        "  srv.Release(k);\n"
+        "  return r;\n"
+        "}\n")
     proc = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", f"-I{ROOT / 'include'}", "-I/usr/local/cuda/include",
                            str(src)], capture_output=True, text=True)
     assert proc.returncode == 0, proc.stderr
