@@ -535,7 +535,7 @@ def run_served(args, world, rank, local):
     gaps = rng.exponential(1.0 / rate, size=total)
 
     def run_pass(on_device: bool):
-        srv = nxb.Server(budget_bytes=32 << 30)
+        srv = nxb.Server(budget_bytes=32 << 30, reserve=True)
         lat, queue, batched = [], [], 0
         tickets = []
         done = threading.Event()

@@ -395,8 +395,12 @@ typedef struct nxb_server_config {
     uint32_t streams;           /* builds in flight at once (0 = 4) */
     uint32_t batch_max_prims;   /* requests up to this size may share a batched build (0 = 65536; 1 = never) */
     uint32_t batch_max_meshes;  /* meshes per batched build (0 = 256) */
-    uint32_t flags;             /* reserved, must be 0 */
+    uint32_t flags;             /* NXB_SERVER_* bits */
 } nxb_server_config;
+
+/* Reserve the whole budget in the server's memory pool at creation, so that
+ * no request waits for the pool to grow (creation then takes longer). */
+#define NXB_SERVER_RESERVE 0x1u
 
 typedef struct nxb_server_result {
     nxb_bvh8 bvh8;          /* device arrays owned by the server until nxb_server_release */

@@ -122,6 +122,7 @@ assert ctypes.sizeof(CBVH2) == 40 and ctypes.sizeof(CBVH8) == 56 and ctypes.size
 assert ctypes.sizeof(CBatchMesh) == 52
 NXB_TUNE_RADIUS = 0x1
 NXB_BUILD_AUCTION = 0x1
+NXB_SERVER_RESERVE = 0x1
 
 _P = ctypes.c_void_p
 _U32 = ctypes.c_uint32
@@ -484,9 +485,10 @@ class Server:
     memory until ``release``.
     """
 
-    def __init__(self, budget_bytes: int = 0, streams: int = 0, batch_max_prims: int = 0, batch_max_meshes: int = 0):
+    def __init__(self, budget_bytes: int = 0, streams: int = 0, batch_max_prims: int = 0, batch_max_meshes: int = 0,
+                 reserve: bool = False):
         self._h = ctypes.c_void_p()
-        c = CServerConfig(budget_bytes, streams, batch_max_prims, batch_max_meshes, 0)
+        c = CServerConfig(budget_bytes, streams, batch_max_prims, batch_max_meshes, NXB_SERVER_RESERVE if reserve else 0)
         check(load().nxb_server_create(ctypes.byref(c), ctypes.byref(self._h)), "nxb_server_create")
         self._keep = {}
 

@@ -407,7 +407,7 @@ nxb_status nxb_server_create(const nxb_server_config* config, nxb_server** out) 
     if (!out) return NXB_ERR_INVALID_ARGUMENT;
     *out = nullptr;
     nxb_server_config c = config ? *config : nxb_server_config{};
-    if (c.flags) return NXB_ERR_UNSUPPORTED;
+    if (c.flags & ~NXB_SERVER_RESERVE) return NXB_ERR_UNSUPPORTED;
     if (c.memory_budget_bytes == 0) c.memory_budget_bytes = 32ull << 30;
     if (c.streams == 0) c.streams = 4;
     if (c.streams > 64) return NXB_ERR_UNSUPPORTED;
@@ -435,6 +435,14 @@ nxb_status nxb_server_create(const nxb_server_config* config, nxb_server** out) 
         if (!e) e = cudaMallocHost(&sl.h_off, 4ull * (c.batch_max_meshes + 1));
         if (!e) e = cudaMallocHost(&sl.h_off8, 4ull * (c.batch_max_meshes + 1));
         if (!e) e = cudaMallocHost(&sl.h_meshes, sizeof(nxb_batch_mesh) * c.batch_max_meshes);
+    }
+    if (!e && (c.flags & NXB_SERVER_RESERVE)) {
+        // take the whole budget into the pool once (it keeps up to the
+        // budget when freed), so that no request waits on the pool growing
+        void* p = nullptr;
+        e = cudaMallocFromPoolAsync(&p, c.memory_budget_bytes, s->pool, s->release_stream);
+        if (!e) e = cudaFreeAsync(p, s->release_stream);
+        if (!e) e = cudaStreamSynchronize(s->release_stream);
     }
     if (e) {
         const nxb_status st = record_cuda_error(e);

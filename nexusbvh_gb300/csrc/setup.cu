@@ -245,29 +245,57 @@ __global__ __launch_bounds__(kThreads) void sort_histogram_kernel(const K* __res
 }
 
 // ---------------------------------------------------------------- batches
-// Mesh of element g, searched between the meshes of the warp's first and
-// last elements (usually the same one).
-__device__ __forceinline__ MeshSpan warp_mesh(const MeshBatch& b, uint32_t wfirst, uint32_t wlast, uint32_t g) {
-    const uint32_t lo = owner_of(b.off, 0, b.meshes - 1, wfirst);
-    const uint32_t hi = owner_of(b.off, lo, b.meshes - 1, wlast);
-    return b.span(owner_of(b.off, lo, hi, g));
+// The meshes of a tile's first and last element, found once per tile by
+// thread 0 (a mesh usually covers many tiles, so both are the same).
+__device__ __forceinline__ void tile_meshes(const MeshBatch& b, uint32_t first, uint32_t last, uint32_t* s_rng) {
+    const uint32_t lo = owner_of(b.off, 0, b.meshes - 1, first);
+    s_rng[0] = lo;
+    s_rng[1] = owner_of(b.off, lo, b.meshes - 1, last);
+}
+
+__device__ __forceinline__ void ord_max(uint32_t* o, const Box& b) {
+    atomicMax(o + 0, ~f2ord(b.mn.x));
+    atomicMax(o + 1, ~f2ord(b.mn.y));
+    atomicMax(o + 2, ~f2ord(b.mn.z));
+    atomicMax(o + 3, f2ord(b.mx.x));
+    atomicMax(o + 4, f2ord(b.mx.y));
+    atomicMax(o + 5, f2ord(b.mx.z));
+}
+
+__device__ __forceinline__ void warp_reduce_box(Box& b) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        Box other;
+        other.mn.x = __shfl_down_sync(kFullMask, b.mn.x, o);
+        other.mn.y = __shfl_down_sync(kFullMask, b.mn.y, o);
+        other.mn.z = __shfl_down_sync(kFullMask, b.mn.z, o);
+        other.mx.x = __shfl_down_sync(kFullMask, b.mx.x, o);
+        other.mx.y = __shfl_down_sync(kFullMask, b.mx.y, o);
+        other.mx.z = __shfl_down_sync(kFullMask, b.mx.z, o);
+        grow(b, other);
+    }
 }
 
 // Stage 1 over a batch: the same tile staging; mesh m's leaves go to BVH2
-// nodes [2*off[m], 2*off[m] + count) with mesh-local primitive indices, and
-// each mesh's box is reduced per warp into scene_ord[6m .. 6m+5] (a warp
-// that spans two meshes falls back to per-lane atomics).
+// nodes [2*off[m], 2*off[m] + count) with mesh-local primitive indices.  A
+// tile inside one mesh reduces its box over the CTA into one set of 6
+// atomics on scene_ord[6m .. 6m+5]; a tile that spans meshes (about one per
+// mesh boundary) reduces per warp, or per lane where a warp spans meshes.
 template <int FLOATS>
 __global__ __launch_bounds__(kThreads) void batch_bounds_kernel(const float* __restrict__ prims, MeshBatch batch,
                                                                 uint32_t total, Node2* __restrict__ nodes,
                                                                 uint32_t* scene_ord, bool aligned16) {
     __shared__ __align__(16) float tile[kThreads * FLOATS];
+    __shared__ uint32_t s_rng[2];
+    __shared__ float s_red[kThreads / 32][6];
     const uint32_t tiles = (total + kThreads - 1) / kThreads;
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
     for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x) {
         const uint32_t first = t * kThreads;
         const uint32_t cnt = min((uint32_t)kThreads, total - first);
         const float* src = prims + (size_t)first * FLOATS;
         __syncthreads();
+        if (threadIdx.x == 0) tile_meshes(batch, first, first + cnt - 1, s_rng);
         if (cnt == kThreads && aligned16) {
             constexpr int V = kThreads * FLOATS / 4;
             const float4* s4 = reinterpret_cast<const float4*>(src);
@@ -278,11 +306,10 @@ __global__ __launch_bounds__(kThreads) void batch_bounds_kernel(const float* __r
             for (uint32_t v = threadIdx.x; v < cnt * FLOATS; v += kThreads) tile[v] = __ldcs(src + v);
         }
         __syncthreads();
-        const uint32_t wfirst = threadIdx.x & ~31u;
-        if (wfirst >= cnt) continue;  // warp-uniform
+        const uint32_t lo = s_rng[0], hi = s_rng[1];
         const bool valid = threadIdx.x < cnt;
         const uint32_t g = first + min(threadIdx.x, cnt - 1);
-        const MeshSpan me = warp_mesh(batch, first + wfirst, first + min(wfirst + 31, cnt - 1), g);
+        const MeshSpan me = batch.span(lo == hi ? lo : owner_of(batch.off, lo, hi, g));
         Box b;
         b.mn = make_float3(3.402823466e+38f, 3.402823466e+38f, 3.402823466e+38f);
         b.mx = make_float3(-3.402823466e+38f, -3.402823466e+38f, -3.402823466e+38f);
@@ -301,36 +328,31 @@ __global__ __launch_bounds__(kThreads) void batch_bounds_kernel(const float* __r
             const uint32_t local = g - me.start;
             store_node(nodes, 2 * me.start + local, b, kInvalid, local);
         }
-        const uint32_t m0 = __shfl_sync(kFullMask, me.m, 0);
-        if (__all_sync(kFullMask, !valid || me.m == m0)) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                Box other;
-                other.mn.x = __shfl_down_sync(kFullMask, b.mn.x, o);
-                other.mn.y = __shfl_down_sync(kFullMask, b.mn.y, o);
-                other.mn.z = __shfl_down_sync(kFullMask, b.mn.z, o);
-                other.mx.x = __shfl_down_sync(kFullMask, b.mx.x, o);
-                other.mx.y = __shfl_down_sync(kFullMask, b.mx.y, o);
-                other.mx.z = __shfl_down_sync(kFullMask, b.mx.z, o);
-                grow(b, other);
+        if (lo == hi) {  // CTA-uniform
+            warp_reduce_box(b);
+            if (lane == 0) {
+                s_red[warp][0] = b.mn.x;
+                s_red[warp][1] = b.mn.y;
+                s_red[warp][2] = b.mn.z;
+                s_red[warp][3] = b.mx.x;
+                s_red[warp][4] = b.mx.y;
+                s_red[warp][5] = b.mx.z;
             }
-            if (lane_id() == 0) {
-                uint32_t* o = scene_ord + 6ull * m0;
-                atomicMax(o + 0, ~f2ord(b.mn.x));
-                atomicMax(o + 1, ~f2ord(b.mn.y));
-                atomicMax(o + 2, ~f2ord(b.mn.z));
-                atomicMax(o + 3, f2ord(b.mx.x));
-                atomicMax(o + 4, f2ord(b.mx.y));
-                atomicMax(o + 5, f2ord(b.mx.z));
+            __syncthreads();
+            if (threadIdx.x < 6) {
+                const int a = threadIdx.x;
+                float v = s_red[0][a];
+                for (int w = 1; w < kThreads / 32; ++w) v = a < 3 ? fminf(v, s_red[w][a]) : fmaxf(v, s_red[w][a]);
+                atomicMax(scene_ord + 6ull * lo + a, a < 3 ? ~f2ord(v) : f2ord(v));
             }
-        } else if (valid) {
-            uint32_t* o = scene_ord + 6ull * me.m;
-            atomicMax(o + 0, ~f2ord(b.mn.x));
-            atomicMax(o + 1, ~f2ord(b.mn.y));
-            atomicMax(o + 2, ~f2ord(b.mn.z));
-            atomicMax(o + 3, f2ord(b.mx.x));
-            atomicMax(o + 4, f2ord(b.mx.y));
-            atomicMax(o + 5, f2ord(b.mx.z));
+        } else {
+            const uint32_t m0 = __shfl_sync(kFullMask, me.m, 0);
+            if (__all_sync(kFullMask, !valid || me.m == m0)) {
+                warp_reduce_box(b);
+                if (lane == 0 && first + (threadIdx.x & ~31u) < first + cnt) ord_max(scene_ord + 6ull * m0, b);
+            } else if (valid) {
+                ord_max(scene_ord + 6ull * me.m, b);
+            }
         }
     }
 }
@@ -338,34 +360,55 @@ __global__ __launch_bounds__(kThreads) void batch_bounds_kernel(const float* __r
 // Stage 2 over a batch: 30-bit codes from each mesh's own box, written as
 // one sort key mesh << 32 | code, the value being the mesh-local primitive
 // index; digit histograms of every pass of that key fused as in the plain
-// kernel, and the same fill work (parent slots, look-back flags).
+// kernel, and the same fill work (parent slots, look-back flags).  Tiles of
+// 256 elements: a tile inside one mesh reads the mesh's span and scene box
+// once, into shared memory.
 template <bool HIST>
 __global__ __launch_bounds__(kThreads) void batch_morton_kernel(const Node2* __restrict__ nodes, MeshBatch batch,
                                                                 uint32_t total, const uint32_t* scene_ord,
                                                                 uint64_t* __restrict__ keys, uint32_t* vals,
                                                                 uint32_t* hist, MortonArgs a) {
     __shared__ uint32_t s_hist[HIST ? kMaxSortPasses * kRadixBins : 1];
+    __shared__ uint32_t s_rng[2];
+    __shared__ float s_scene[6];
     if (HIST)
         for (int i = threadIdx.x; i < a.pd.passes * kRadixBins; i += kThreads) s_hist[i] = 0;
-    __syncthreads();
-    const uint32_t lane = lane_id();
+    const uint32_t tiles = (total + kThreads - 1) / kThreads;
     const uint32_t stride = gridDim.x * kThreads;
-    for (uint32_t base = blockIdx.x * kThreads + (threadIdx.x & ~31u); base < total; base += stride) {
-        const uint32_t i = base + lane;
-        const bool valid = i < total;
+    for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+        const uint32_t first = t * kThreads;
+        const uint32_t cnt = min((uint32_t)kThreads, total - first);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            tile_meshes(batch, first, first + cnt - 1, s_rng);
+            if (s_rng[0] == s_rng[1]) {
+                const uint32_t* o = scene_ord + 6ull * s_rng[0];
+                for (int k = 0; k < 6; ++k) s_scene[k] = ord2f(k < 3 ? ~o[k] : o[k]);
+            }
+        }
+        __syncthreads();
+        const uint32_t lo = s_rng[0], hi = s_rng[1];
+        const uint32_t i = first + threadIdx.x;
+        const bool valid = threadIdx.x < cnt;
         uint64_t key = 0;
         if (valid) {
-            const MeshSpan me = warp_mesh(batch, base, min(base + 31, total - 1), i);
+            const MeshSpan me = batch.span(lo == hi ? lo : owner_of(batch.off, lo, hi, i));
+            float3 smin, smax;
+            if (lo == hi) {
+                smin = make_float3(s_scene[0], s_scene[1], s_scene[2]);
+                smax = make_float3(s_scene[3], s_scene[4], s_scene[5]);
+            } else {
+                const uint32_t* o = scene_ord + 6ull * me.m;
+                smin = make_float3(ord2f(~__ldg(o + 0)), ord2f(~__ldg(o + 1)), ord2f(~__ldg(o + 2)));
+                smax = make_float3(ord2f(__ldg(o + 3)), ord2f(__ldg(o + 4)), ord2f(__ldg(o + 5)));
+            }
             const uint32_t local = i - me.start;
-            const uint32_t* o = scene_ord + 6ull * me.m;
-            const float3 smin = make_float3(ord2f(~__ldg(o + 0)), ord2f(~__ldg(o + 1)), ord2f(~__ldg(o + 2)));
-            const float3 smax = make_float3(ord2f(__ldg(o + 3)), ord2f(__ldg(o + 4)), ord2f(__ldg(o + 5)));
             const float4* p = reinterpret_cast<const float4*>(nodes + 2ull * me.start + local);
-            float4 lo = __ldcs(p);
-            float2 hi = __ldcs(reinterpret_cast<const float2*>(p + 1));
+            float4 lo4 = __ldcs(p);
+            float2 hi2 = __ldcs(reinterpret_cast<const float2*>(p + 1));
             Box b;
-            b.mn = make_float3(lo.x, lo.y, lo.z);
-            b.mx = make_float3(lo.w, hi.x, hi.y);
+            b.mn = make_float3(lo4.x, lo4.y, lo4.z);
+            b.mx = make_float3(lo4.w, hi2.x, hi2.y);
             key = ((uint64_t)me.m << 32) | morton_key<uint32_t>(b, smin, smax);
             keys[i] = key;
             vals[i] = local;

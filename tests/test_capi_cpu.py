@@ -136,7 +136,7 @@ def test_batch_argument_checks_need_no_device(lib):
 
 def test_server_argument_checks_need_no_device(lib):
     h = ctypes.c_void_p()
-    bad = nxb.CServerConfig(0, 0, 0, 0, 1)
+    bad = nxb.CServerConfig(0, 0, 0, 0, 2)
     assert lib.nxb_server_create(ctypes.byref(bad), ctypes.byref(h)) == 2
     many = nxb.CServerConfig(0, 65, 0, 0, 0)
     assert lib.nxb_server_create(ctypes.byref(many), ctypes.byref(h)) == 2
