@@ -356,6 +356,26 @@ def run_batch(args, world, rank, local):
     t_tune = time.perf_counter()
     tuning = batch.tuning() if args.no_autotune else batch.autotune(d_prims, repeats=2)
     t_tune = time.perf_counter() - t_tune
+
+    def timed_build(fuse: int, reps: int = 5) -> float:
+        """Median ms of a build with the chosen tuning but the given fusion point."""
+        t = batch.tuning()
+        t.fuse_bvh8 = fuse
+        batch.set_tuning(t)
+        batch.build(d_prims)
+        ms = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            batch.build_async(d_prims)
+            e1.record()
+            batch.wait(results=False)
+            ms.append(e0.elapsed_time(e1))
+        return statistics.median(ms)
+
+    chosen = batch.tuning()
+    fusion = {"collapse_after_hploc_ms": round(timed_build(0), 4), "collapse_alongside_hploc_ms": round(timed_build(1), 4)}
+    batch.set_tuning(chosen)
     for _ in range(args.warmup):
         batch.build_async(d_prims)
     batch.wait(results=False)
@@ -462,6 +482,7 @@ def run_batch(args, world, rank, local):
             "l2": "inputs larger than L2 (1.3 GB of triangles), no flush needed",
             "tuning": {"sort_digit_bits": int(tuning.sort_digit_bits), "sort_passes": passes,
                        "hploc_ctas_per_sm": int(tuning.hploc_ctas_per_sm),
+                       "fuse_bvh8": int(tuning.fuse_bvh8), "fusion_point": fusion,
                        "candidates": int(tuning.candidates_tried), "tune_s": round(t_tune, 2)},
             "bvh8_nodes": int(n8),
             "loop_plain_api_ms": _num(t_loop * 1e3),

@@ -339,6 +339,9 @@ typedef struct nxb_batch_tuning {
     uint32_t sort_digit_bits;   /* 5..8: bits per radix sort pass */
     uint32_t search_radius;     /* H-PLOC radius in use */
     uint32_t hploc_ctas_per_sm; /* cap on the H-PLOC persistent grid (0 = occupancy) */
+    uint32_t fuse_bvh8;         /* BVH2/BVH8 fusion point: 0 = collapse after H-PLOC has built every
+                                   mesh; 1 = collapse each mesh as soon as H-PLOC publishes its root,
+                                   running alongside H-PLOC */
     uint32_t candidates_tried;
     float build_ms;             /* median time of one build with these settings */
 } nxb_batch_tuning;
@@ -368,7 +371,7 @@ nxb_status nxb_batch_get_arrays(const nxb_batch* batch, nxb_batch_arrays* out_ar
 /* Times candidate settings on this batch and input (each: one warm-up build,
  * then the median of `repeats` builds) and keeps the fastest.  Without
  * NXB_TUNE_RADIUS only settings that leave the results unchanged are tried
- * (sort digit width, H-PLOC grid size). */
+ * (sort digit width, H-PLOC grid size, BVH2/BVH8 fusion point). */
 nxb_status nxb_batch_autotune(nxb_batch* batch, const void* d_prims, uint32_t tune_flags, uint32_t repeats,
                               struct CUstream_st* stream, nxb_batch_tuning* out_choice);
 nxb_status nxb_batch_set_tuning(nxb_batch* batch, const nxb_batch_tuning* tuning);

@@ -129,7 +129,8 @@ void batch_bind(unsigned char* p, BatchArena* a) {
 }
 
 nxb_status batch_enqueue(const BatchArena& a, const void* prims, nxb_prim_type type, const BatchTuning& t,
-                         uint32_t* h_err, cudaStream_t s) {
+                         uint32_t* h_err, cudaStream_t s, const BatchFork* fork) {
+    const bool fused = t.fuse && fork && a.total > 0;
     const MeshBatch mb{a.off, a.off8, a.meshes};
     const SortPlan plan = make_sort_plan(2, 32 + a.mesh_bits, t.digit_bits);
     NXB_TRY(cudaMemsetAsync(a.zero_begin, 0, a.zero_bytes, s));
@@ -153,13 +154,28 @@ nxb_status batch_enqueue(const BatchArena& a, const void* prims, nxb_prim_type t
         uint64_t* keys = in_a ? a.keys_a : a.keys_b;
         uint32_t* perm = in_a ? a.vals_a : a.vals_b;
         uint32_t* tokens = in_a ? a.vals_b : a.vals_a;
+        if (fused) {
+            // the collapse starts on the side stream and takes each mesh's
+            // root item as H-PLOC publishes it
+            NXB_TRY(launch_bvh8_batch_init(a.pairs, a.slots, mb, a.ctr8, a.mesh_nodes, a.mesh_leaves, true, s));
+            NXB_TRY(cudaEventRecord(fork->fork, s));
+            NXB_TRY(cudaStreamWaitEvent(fork->side, fork->fork, 0));
+            NXB_TRY(launch_bvh8_batch(a.bvh2, mb, a.total, a.bvh8, a.slots, a.prim_idx, a.pairs, a.ctr8,
+                                      a.mesh_nodes, a.mesh_leaves, &a.ctrl->error_word, t.auction, true, fork->side));
+            NXB_TRY(cudaEventRecord(fork->join, fork->side));
+        }
         NXB_TRY(launch_hploc_batch(keys, perm, a.parent, a.bvh2, mb, a.total, t.radius, tokens, a.pol,
-                                   &a.ctrl->leaf_ctr, &a.ctrl->error_word, t.hploc_ctas_per_sm, s));
+                                   &a.ctrl->leaf_ctr, &a.ctrl->error_word, t.hploc_ctas_per_sm,
+                                   fused ? a.pairs : nullptr, s));
     }
-    NXB_TRY(launch_bvh8_batch_init(a.pairs, a.slots, mb, a.ctr8, a.mesh_nodes, a.mesh_leaves, s));
-    if (a.total > 0)
-        NXB_TRY(launch_bvh8_batch(a.bvh2, mb, a.total, a.bvh8, a.slots, a.prim_idx, a.pairs, a.ctr8, a.mesh_nodes,
-                                  a.mesh_leaves, &a.ctrl->error_word, t.auction, s));
+    if (fused) {
+        NXB_TRY(cudaStreamWaitEvent(s, fork->join, 0));
+    } else {
+        NXB_TRY(launch_bvh8_batch_init(a.pairs, a.slots, mb, a.ctr8, a.mesh_nodes, a.mesh_leaves, false, s));
+        if (a.total > 0)
+            NXB_TRY(launch_bvh8_batch(a.bvh2, mb, a.total, a.bvh8, a.slots, a.prim_idx, a.pairs, a.ctr8,
+                                      a.mesh_nodes, a.mesh_leaves, &a.ctrl->error_word, t.auction, false, s));
+    }
     NXB_TRY(launch_batch_finalize(mb, a.scene_ord, a.mesh_nodes, a.mesh_leaves, a.results, s));
     if (h_err)
         NXB_TRY(cudaMemcpyAsync(h_err, &a.ctrl->error_word, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -178,6 +194,7 @@ struct nxb_batch {
     unsigned char* mem = nullptr;
     uint32_t* h_err = nullptr;  // pinned; the graph copies the error word here
     cudaStream_t cap_stream = nullptr;
+    BatchFork fork{nullptr, nullptr, nullptr};  // side stream of a fused capture
     cudaGraphExec_t exec = nullptr;
     const void* graph_prims = nullptr;
     bool graph_valid = false;
@@ -197,13 +214,15 @@ BatchTuning tuning_of(const nxb_batch_tuning& t, bool auction) {
     r.digit_bits = t.sort_digit_bits;
     r.radius = t.search_radius;
     r.hploc_ctas_per_sm = t.hploc_ctas_per_sm;
+    r.fuse = t.fuse_bvh8 != 0;
     return r;
 }
 
 nxb_status capture(nxb_batch* b, const void* prims) {
     cudaGraph_t g = nullptr;
     NXB_TRY(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeRelaxed));
-    const nxb_status st = batch_enqueue(b->arena, prims, b->type, tuning_of(b->tuning, b->auction), b->h_err, b->cap_stream);
+    const nxb_status st =
+        batch_enqueue(b->arena, prims, b->type, tuning_of(b->tuning, b->auction), b->h_err, b->cap_stream, &b->fork);
     const cudaError_t ec = cudaStreamEndCapture(b->cap_stream, &g);
     if (st != NXB_OK) {
         if (g) cudaGraphDestroy(g);
@@ -230,6 +249,9 @@ nxb_status capture(nxb_batch* b, const void* prims) {
 void release(nxb_batch* b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+    if (b->fork.side) cudaStreamDestroy(b->fork.side);
+    if (b->fork.fork) cudaEventDestroy(b->fork.fork);
+    if (b->fork.join) cudaEventDestroy(b->fork.join);
     if (b->h_err) cudaFreeHost(b->h_err);
     if (b->mem) cudaFree(b->mem);
     delete b;
@@ -265,6 +287,9 @@ nxb_status nxb_batch_create(nxb_prim_type type, const uint32_t* h_off, uint32_t 
     cudaError_t e = cudaMalloc(&b->mem, b->arena.bytes);
     if (!e) e = cudaMallocHost(&b->h_err, sizeof(uint32_t));
     if (!e) e = cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking);
+    if (!e) e = cudaStreamCreateWithFlags(&b->fork.side, cudaStreamNonBlocking);
+    if (!e) e = cudaEventCreateWithFlags(&b->fork.fork, cudaEventDisableTiming);
+    if (!e) e = cudaEventCreateWithFlags(&b->fork.join, cudaEventDisableTiming);
     if (!e) {
         batch_bind(b->mem, &b->arena);
         e = cudaMemcpy(b->arena.off, h_off, 4ull * (meshes + 1), cudaMemcpyHostToDevice);
@@ -334,6 +359,7 @@ nxb_status nxb_batch_set_tuning(nxb_batch* b, const nxb_batch_tuning* t) {
     b->tuning.sort_digit_bits = t->sort_digit_bits;
     b->tuning.search_radius = t->search_radius;
     b->tuning.hploc_ctas_per_sm = t->hploc_ctas_per_sm;
+    b->tuning.fuse_bvh8 = t->fuse_bvh8 ? 1u : 0u;
     b->graph_valid = false;
     return NXB_OK;
 }
@@ -356,6 +382,7 @@ nxb_status nxb_batch_autotune(nxb_batch* b, const void* prims, uint32_t flags, u
         radii = {b->tuning.search_radius};
     const uint32_t digits[] = {8, 7, 6, 5};
     const uint32_t ctas[] = {0, 4};
+    const uint32_t fuses[] = {0, 1};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     NXB_TRY(cudaEventCreate(&e0));
     const cudaError_t ce = cudaEventCreate(&e1);
@@ -371,11 +398,13 @@ nxb_status nxb_batch_autotune(nxb_batch* b, const void* prims, uint32_t flags, u
     for (uint32_t r : radii) {
         for (uint32_t d : digits) {
             if (!batch_digit_ok(b->arena.mesh_bits, d)) continue;
-            for (uint32_t c : ctas) {
+            for (uint32_t c : ctas)
+            for (uint32_t f : fuses) {
                 nxb_batch_tuning t = start;
                 t.sort_digit_bits = d;
                 t.search_radius = r;
                 t.hploc_ctas_per_sm = c;
+                t.fuse_bvh8 = f;
                 if ((st = nxb_batch_set_tuning(b, &t)) != NXB_OK) break;
                 if ((st = nxb_batch_build(b, prims, s, nullptr)) != NXB_OK) break;  // capture + warm-up
                 std::vector<float> ms;

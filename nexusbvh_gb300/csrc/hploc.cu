@@ -84,6 +84,8 @@ struct MergeCtx {
     uint32_t n;
     uint32_t node_limit;       // 2n-1
     uint32_t* err;
+    uint64_t* publish;         // batched, BVH8 running alongside: the mesh's BVH8 root item slot
+    uint64_t item;             // ... and the item written there once the root is stored
 };
 
 // One round of PLOC merging (MergeClustersCreateBVH2Node,
@@ -175,12 +177,16 @@ __device__ __forceinline__ void merge_root(const MergeCtx& m, uint32_t& cid, uin
 // The mesh of the owner lane: `all` holds the bases of the concatenated
 // arrays; the context returned addresses this mesh's nodes and counter.
 template <typename Seg>
-__device__ __forceinline__ MergeCtx mesh_ctx(const MergeCtx& all, MeshSpan me, uint32_t owner, uint32_t& start) {
+__device__ __forceinline__ MergeCtx mesh_ctx(const MergeCtx& all, const Seg& seg, MeshSpan me, uint32_t owner,
+                                             uint32_t& start) {
     if constexpr (Seg::kBatch) {
         const uint32_t mesh = __shfl_sync(kFullMask, me.m, owner);
         start = __shfl_sync(kFullMask, me.start, owner);
         const uint32_t count = __shfl_sync(kFullMask, me.count, owner);
-        return MergeCtx{all.nodes + 2ull * start, all.tok, all.parent_of_last + mesh, count, 2 * count - 1, all.err};
+        uint64_t* pub = all.publish ? all.publish + mesh : nullptr;
+        const uint64_t item = pub ? ((uint64_t)(2 * count - 2) << 32) | __ldg(seg.off8 + mesh) : 0ull;
+        return MergeCtx{all.nodes + 2ull * start, all.tok, all.parent_of_last + mesh, count, 2 * count - 1, all.err,
+                        pub, item};
     } else {
         start = 0;
         return all;
@@ -245,6 +251,11 @@ __device__ __forceinline__ void merge_windows(uint32_t owner, uint32_t left, uin
     while (num > threshold) {
         if (fin && num == 2) {
             merge_root(m, cid, ctok, cb);
+            if (m.publish && lane == 0) {
+                // the tree is complete: hand its root to the BVH8 collapse
+                fence_acq_rel_gpu();
+                st_relaxed_u64(m.publish, m.item);
+            }
             num = 1;
             break;
         }
@@ -261,10 +272,10 @@ __device__ __forceinline__ void merge_windows(uint32_t owner, uint32_t left, uin
 // Out of line: the climb loop stays small and the merge gets the registers.
 template <int R, typename Seg>
 __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t right, uint32_t split, bool final,
-                                        MeshSpan me, uint32_t* cluster, const MergeCtx& all) {
+                                        MeshSpan me, uint32_t* cluster, const MergeCtx& all, const Seg& seg) {
     if constexpr (Seg::kBatch) {
         uint32_t start;
-        const MergeCtx m = mesh_ctx<Seg>(all, me, owner, start);
+        const MergeCtx m = mesh_ctx<Seg>(all, seg, me, owner, start);
         merge_windows<R>(owner, left, right, split, final, start, cluster, m);
     } else {
         merge_windows<R>(owner, left, right, split, final, 0u, cluster, all);
@@ -292,9 +303,9 @@ template <typename K, int R, typename Seg>
 __global__ __launch_bounds__(kThreads, 12) void hploc_kernel(const K* __restrict__ keys, uint32_t* cluster,
                                                          uint32_t* parent, Node2* nodes, Seg seg, uint32_t total,
                                                          uint32_t* tok, uint32_t* parent_of_last, uint32_t* leaf_ctr,
-                                                         uint32_t* err) {
+                                                         uint32_t* err, uint64_t* publish) {
     const uint32_t lane = lane_id();
-    const MergeCtx all{nodes, tok, parent_of_last, total, 2 * total - 1, err};
+    const MergeCtx all{nodes, tok, parent_of_last, total, 2 * total - 1, err, publish, 0ull};
     uint32_t left = 0, right = 0, split = 0;
     // the lane's mesh; a plain build has one, known at compile time
     MeshSpan me = Seg::kBatch ? MeshSpan{0, 0, 0} : seg.of_prim(0);
@@ -357,7 +368,7 @@ __global__ __launch_bounds__(kThreads, 12) void hploc_kernel(const K* __restrict
             fence_acq_rel_gpu();  // acquire: the siblings' clusters
             while (todo) {
                 const uint32_t owner = __ffs(todo) - 1;
-                ploc_merge<R, Seg>(owner, left, right, split, final, me, cluster, all);
+                ploc_merge<R, Seg>(owner, left, right, split, final, me, cluster, all, seg);
                 todo &= todo - 1;
             }
             __syncwarp();
@@ -369,7 +380,7 @@ __global__ __launch_bounds__(kThreads, 12) void hploc_kernel(const K* __restrict
 template <typename K, int R, typename Seg>
 cudaError_t launch_r(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, Seg seg, uint32_t total,
                      uint32_t* tok, uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err, uint32_t max_per_sm,
-                     cudaStream_t s) {
+                     uint64_t* publish, cudaStream_t s) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hploc_kernel<K, R, Seg>, kThreads, 0);
     if (max_per_sm && (uint32_t)per_sm > max_per_sm) per_sm = (int)max_per_sm;
@@ -377,19 +388,24 @@ cudaError_t launch_r(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* 
     const uint32_t want = (total + kThreads - 1) / kThreads;
     const uint32_t grid = std::max(1u, std::min(want, (uint32_t)(device_info().sms * per_sm)));
     hploc_kernel<K, R, Seg><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, seg, total, tok, pol, leaf_ctr,
-                                                      err);
+                                                      err, publish);
     return cudaGetLastError();
 }
 
 template <typename K, typename Seg>
 cudaError_t launch_t(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, Seg seg, uint32_t total,
                      uint32_t radius, uint32_t* tok, uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err,
-                     uint32_t max_per_sm, cudaStream_t s) {
+                     uint32_t max_per_sm, uint64_t* publish, cudaStream_t s) {
     switch (radius) {
-        case 4: return launch_r<K, 4>(keys, cluster, parent, nodes, seg, total, tok, pol, leaf_ctr, err, max_per_sm, s);
+        case 4:
+            return launch_r<K, 4>(keys, cluster, parent, nodes, seg, total, tok, pol, leaf_ctr, err, max_per_sm,
+                                  publish, s);
         case 16:
-            return launch_r<K, 16>(keys, cluster, parent, nodes, seg, total, tok, pol, leaf_ctr, err, max_per_sm, s);
-        default: return launch_r<K, 8>(keys, cluster, parent, nodes, seg, total, tok, pol, leaf_ctr, err, max_per_sm, s);
+            return launch_r<K, 16>(keys, cluster, parent, nodes, seg, total, tok, pol, leaf_ctr, err, max_per_sm,
+                                   publish, s);
+        default:
+            return launch_r<K, 8>(keys, cluster, parent, nodes, seg, total, tok, pol, leaf_ctr, err, max_per_sm,
+                                  publish, s);
     }
 }
 
@@ -401,17 +417,17 @@ cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster
     const SingleMesh seg{n};
     if (key_bytes == 4)
         return launch_t((const uint32_t*)keys, cluster_idx, parent, nodes, seg, n, radius, tokens, parent_of_last,
-                        leaf_ctr, err, 0u, s);
+                        leaf_ctr, err, 0u, nullptr, s);
     return launch_t((const uint64_t*)keys, cluster_idx, parent, nodes, seg, n, radius, tokens, parent_of_last,
-                    leaf_ctr, err, 0u, s);
+                    leaf_ctr, err, 0u, nullptr, s);
 }
 
 cudaError_t launch_hploc_batch(const uint64_t* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
                                const MeshBatch& batch, uint32_t total, uint32_t radius, uint32_t* tokens,
                                uint32_t* parent_of_last, uint32_t* leaf_ctr, uint32_t* err, uint32_t ctas_per_sm,
-                               cudaStream_t s) {
+                               uint64_t* publish, cudaStream_t s) {
     return launch_t(reinterpret_cast<const MeshKey*>(keys), cluster_idx, parent, nodes, batch, total, radius, tokens,
-                    parent_of_last, leaf_ctr, err, ctas_per_sm, s);
+                    parent_of_last, leaf_ctr, err, ctas_per_sm, publish, s);
 }
 
 }  // namespace nxb

@@ -119,17 +119,21 @@ cudaError_t launch_batch_morton(const Node2* nodes, const MeshBatch& batch, uint
                                 uint64_t* keys, uint32_t* vals, const SortPlan& plan, uint32_t* hist,
                                 const MortonFused& fill, cudaStream_t s);
 // parent_of_last: one word per mesh holding INVALID on entry; ctas_per_sm
-// caps the persistent grid (0: as many CTAs as fit).
+// caps the persistent grid (0: as many CTAs as fit).  publish (optional):
+// BVH8 item slots, one per mesh; when a mesh's root is stored, its BVH8 root
+// item is written to publish[mesh] (the BVH8 collapse runs alongside).
 cudaError_t launch_hploc_batch(const uint64_t* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
                                const MeshBatch& batch, uint32_t total, uint32_t radius, uint32_t* tokens,
                                uint32_t* parent_of_last, uint32_t* leaf_ctr, uint32_t* err, uint32_t ctas_per_sm,
-                               cudaStream_t s);
+                               uint64_t* publish, cudaStream_t s);
 // pairs: `slots` = off8[meshes] uint64 slots; ctr: kBvh8CtrWords words.
+// fused: the root items of meshes of 2+ primitives are left for H-PLOC to
+// publish, and the collapse runs while H-PLOC still builds other meshes.
 cudaError_t launch_bvh8_batch_init(uint64_t* pairs, uint32_t slots, const MeshBatch& batch, uint32_t* ctr,
-                                   uint32_t* mesh_nodes, uint32_t* mesh_leaves, cudaStream_t s);
+                                   uint32_t* mesh_nodes, uint32_t* mesh_leaves, bool fused, cudaStream_t s);
 cudaError_t launch_bvh8_batch(const Node2* bvh2, const MeshBatch& batch, uint32_t total, Node8* out, uint32_t slots,
                               uint32_t* prim_idx, uint64_t* pairs, uint32_t* ctr, uint32_t* mesh_nodes,
-                              uint32_t* mesh_leaves, uint32_t* err, bool auction, cudaStream_t s);
+                              uint32_t* mesh_leaves, uint32_t* err, bool auction, bool fused, cudaStream_t s);
 cudaError_t launch_batch_finalize(const MeshBatch& batch, const uint32_t* scene_ord, const uint32_t* mesh_nodes,
                                   const uint32_t* mesh_leaves, nxb_batch_mesh* out, cudaStream_t s);
 // One batched build's device memory (a single allocation carved into
@@ -172,6 +176,13 @@ struct BatchArena {
 struct BatchTuning {
     uint32_t digit_bits = 8, radius = 8, hploc_ctas_per_sm = 0;
     bool auction = false;
+    bool fuse = false;  // BVH8 collapse alongside H-PLOC (needs a BatchFork)
+};
+// A second stream and two events for running the BVH8 collapse alongside
+// H-PLOC (BatchTuning::fuse).
+struct BatchFork {
+    cudaStream_t side;
+    cudaEvent_t fork, join;
 };
 // BVH8 node capacity of one mesh (the reference's ceil((4n-1)/7); 1 for an
 // empty mesh, so that BVH8 offsets are strictly increasing).
@@ -183,9 +194,11 @@ bool batch_layout(const uint32_t* h_off, uint32_t meshes, uint32_t* h_off8, Batc
 void batch_bind(unsigned char* base, BatchArena* a);
 bool batch_digit_ok(uint32_t mesh_bits, uint32_t digit_bits);
 // The batched pipeline on stream s; off/off8 must already be on the device.
-// If h_err is not null, the error word is copied there at the end.
+// If h_err is not null, the error word is copied there at the end.  With
+// t.fuse and a fork, the BVH8 collapse runs on fork->side alongside H-PLOC
+// (joined back into s before the end).
 nxb_status batch_enqueue(const BatchArena& a, const void* prims, nxb_prim_type type, const BatchTuning& t,
-                         uint32_t* h_err, cudaStream_t s);
+                         uint32_t* h_err, cudaStream_t s, const BatchFork* fork = nullptr);
 // ---------------------------------------------------------------- eval
 cudaError_t launch_bvh2_cost(const Node2* nodes, uint32_t count, const nxb_aabb* root, float* cost, cudaStream_t s);
 cudaError_t launch_bvh8_cost(const Node8* nodes, uint32_t count, const nxb_aabb* root, float* cost, cudaStream_t s);

@@ -93,6 +93,20 @@ def test_batch_matches_oracle(gpu, orc):
         assert errs8 == 0, rep8
 
 
+def test_batch_fused_collapse_matches_plain_builds(gpu, orc):
+    """BVH2/BVH8 fusion point 1: each mesh's collapse starts when H-PLOC
+    publishes its root, alongside H-PLOC; results equal the plain builds."""
+    prims = make_batch(COUNTS, seed=12)
+    batch = nxb.Batch(COUNTS)
+    t = batch.tuning()
+    t.fuse_bvh8 = 1
+    batch.set_tuning(t)
+    d = S.dev(prims)
+    for _ in range(3):  # capture, then replays
+        meshes = batch.build(d)
+    check_against_plain(batch, meshes, prims, COUNTS, orc)
+
+
 def test_batch_aabb_input(gpu, orc):
     counts = [500, 0, 1, 2000]
     prims = make_batch(counts, seed=9, boxes=True)
@@ -109,9 +123,9 @@ def test_batch_replay_and_tuning_keep_results(gpu, orc):
     first = batch.build(d)
     ref = [(batch.mesh_bvh2_host(m, first).tobytes(), batch.mesh_bvh8_host(m)) for m in range(len(counts))
            if counts[m]]
-    for digits, ctas in ((5, 0), (6, 4), (7, 0), (8, 4)):
+    for digits, ctas, fuse in ((5, 0, 0), (6, 4, 1), (7, 0, 1), (8, 4, 0)):
         t = batch.tuning()
-        t.sort_digit_bits, t.hploc_ctas_per_sm = digits, ctas
+        t.sort_digit_bits, t.hploc_ctas_per_sm, t.fuse_bvh8 = digits, ctas, fuse
         batch.set_tuning(t)
         for _ in range(2):  # capture, then replay
             again = batch.build(d)
