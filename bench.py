@@ -357,10 +357,10 @@ def run_batch(args, world, rank, local):
     tuning = batch.tuning() if args.no_autotune else batch.autotune(d_prims, repeats=2)
     t_tune = time.perf_counter() - t_tune
 
-    def timed_build(fuse: int, reps: int = 5) -> float:
+    def timed_build(groups: int, reps: int = 5) -> float:
         """Median ms of a build with the chosen tuning but the given fusion point."""
         t = batch.tuning()
-        t.fuse_bvh8 = fuse
+        t.fusion_groups = groups
         batch.set_tuning(t)
         batch.build(d_prims)
         ms = []
@@ -374,7 +374,7 @@ def run_batch(args, world, rank, local):
         return statistics.median(ms)
 
     chosen = batch.tuning()
-    fusion = {"collapse_after_hploc_ms": round(timed_build(0), 4), "collapse_alongside_hploc_ms": round(timed_build(1), 4)}
+    fusion = {f"groups_{g}_ms": round(timed_build(g), 4) for g in (1, 2, 4, 8)}
     batch.set_tuning(chosen)
     for _ in range(args.warmup):
         batch.build_async(d_prims)
@@ -482,7 +482,8 @@ def run_batch(args, world, rank, local):
             "l2": "inputs larger than L2 (1.3 GB of triangles), no flush needed",
             "tuning": {"sort_digit_bits": int(tuning.sort_digit_bits), "sort_passes": passes,
                        "hploc_ctas_per_sm": int(tuning.hploc_ctas_per_sm),
-                       "fuse_bvh8": int(tuning.fuse_bvh8), "fusion_point": fusion,
+                       "fusion_groups": int(tuning.fusion_groups), "block_size": int(tuning.block_size),
+                       "fusion_point": fusion,
                        "candidates": int(tuning.candidates_tried), "tune_s": round(t_tune, 2)},
             "bvh8_nodes": int(n8),
             "loop_plain_api_ms": _num(t_loop * 1e3),

@@ -339,9 +339,11 @@ typedef struct nxb_batch_tuning {
     uint32_t sort_digit_bits;   /* 5..8: bits per radix sort pass */
     uint32_t search_radius;     /* H-PLOC radius in use */
     uint32_t hploc_ctas_per_sm; /* cap on the H-PLOC persistent grid (0 = occupancy) */
-    uint32_t fuse_bvh8;         /* BVH2/BVH8 fusion point: 0 = collapse after H-PLOC has built every
-                                   mesh; 1 = collapse each mesh as soon as H-PLOC publishes its root,
-                                   running alongside H-PLOC */
+    uint32_t fusion_groups;     /* BVH2/BVH8 fusion point: 0 or 1 = collapse after H-PLOC has built
+                                   every mesh; 2..8 = meshes cut into that many groups of about equal
+                                   triangle count, the BVH8 collapse of each group running while
+                                   H-PLOC builds the next */
+    uint32_t block_size;        /* threads per CTA of the bounds and Morton kernels: 128, 256 or 512 */
     uint32_t candidates_tried;
     float build_ms;             /* median time of one build with these settings */
 } nxb_batch_tuning;

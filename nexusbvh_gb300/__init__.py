@@ -97,8 +97,9 @@ class CBatchArrays(ctypes.Structure):
 
 class CBatchTuning(ctypes.Structure):
     _fields_ = [("sort_digit_bits", ctypes.c_uint32), ("search_radius", ctypes.c_uint32),
-                ("hploc_ctas_per_sm", ctypes.c_uint32), ("fuse_bvh8", ctypes.c_uint32),
-                ("candidates_tried", ctypes.c_uint32), ("build_ms", ctypes.c_float)]
+                ("hploc_ctas_per_sm", ctypes.c_uint32), ("fusion_groups", ctypes.c_uint32),
+                ("block_size", ctypes.c_uint32), ("candidates_tried", ctypes.c_uint32),
+                ("build_ms", ctypes.c_float)]
 
 
 class CServerConfig(ctypes.Structure):

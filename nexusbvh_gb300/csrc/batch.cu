@@ -59,7 +59,7 @@ Segments segments_of(const BatchArena& a) {
     g.zero_end = at;
     g.parent = seg(4 * (n + M));
     g.look = seg(4 * a.lookback_words_per_pass * kMaxSortPasses);
-    g.ctr8 = seg(4 * kBvh8CtrWords);
+    g.ctr8 = seg(4 * kBvh8CtrWords * kMaxMeshGroups);
     g.mnodes = seg(4 * M);
     g.mleaves = seg(4 * M);
     g.ka = seg(8 * n);
@@ -128,21 +128,44 @@ void batch_bind(unsigned char* p, BatchArena* a) {
     a->results = reinterpret_cast<nxb_batch_mesh*>(p + g.res);
 }
 
+void batch_groups(const uint32_t* h_off, const uint32_t* h_off8, uint32_t meshes, uint32_t want, MeshGroups* g) {
+    want = std::max(1u, std::min(want, kMaxMeshGroups));
+    const uint64_t total = h_off[meshes];
+    g->count = 0;
+    g->mesh[0] = 0;
+    for (uint32_t k = 1; k < want; ++k) {
+        // the first mesh starting at or after k/want of the primitives
+        const uint32_t target = (uint32_t)(total * k / want);
+        const uint32_t m = (uint32_t)(std::lower_bound(h_off, h_off + meshes, target) - h_off);
+        if (m > g->mesh[g->count] && m < meshes) g->mesh[++g->count] = m;
+    }
+    g->mesh[++g->count] = meshes;
+    for (uint32_t k = 0; k <= g->count; ++k) {
+        g->prim[k] = h_off[g->mesh[k]];
+        g->slot[k] = h_off8[g->mesh[k]];
+    }
+}
+
 nxb_status batch_enqueue(const BatchArena& a, const void* prims, nxb_prim_type type, const BatchTuning& t,
-                         uint32_t* h_err, cudaStream_t s, const BatchFork* fork) {
-    const bool fused = t.fuse && fork && a.total > 0;
+                         uint32_t* h_err, cudaStream_t s, const MeshGroups* groups, const BatchFork* fork) {
+    MeshGroups one{};
+    one.count = 1;
+    one.mesh[1] = a.meshes;
+    one.prim[1] = a.total;
+    one.slot[1] = a.slots;
+    const MeshGroups& g = (groups && fork && groups->count > 1) ? *groups : one;
     const MeshBatch mb{a.off, a.off8, a.meshes};
     const SortPlan plan = make_sort_plan(2, 32 + a.mesh_bits, t.digit_bits);
     NXB_TRY(cudaMemsetAsync(a.zero_begin, 0, a.zero_bytes, s));
     if (a.total > 0) {
-        NXB_TRY(launch_batch_bounds(prims, type, mb, a.total, a.bvh2, a.scene_ord, s));
+        NXB_TRY(launch_batch_bounds(prims, type, mb, a.total, a.bvh2, a.scene_ord, t.block, s));
         MortonFused f{};
         f.zero_ptr = a.lookback;
         f.zero_words = align_up(4 * a.lookback_words_per_pass * plan.passes) / 4;
         f.ones_ptr = a.parent;
         f.ones_words = a.ones_words;
         NXB_TRY(launch_batch_morton(a.bvh2, mb, a.total, a.scene_ord, a.keys_a, a.vals_a, plan, &a.ctrl->hist[0][0],
-                                    f, s));
+                                    f, t.block, s));
         for (int p = 0; p < plan.passes; ++p) {
             const bool even = (p % 2) == 0;
             NXB_TRY(launch_sort_pass(8, even ? a.keys_a : a.keys_b, even ? a.keys_b : a.keys_a,
@@ -150,31 +173,35 @@ nxb_status batch_enqueue(const BatchArena& a, const void* prims, nxb_prim_type t
                                      plan.bits[p], a.ctrl->hist[p], a.lookback + p * a.lookback_words_per_pass,
                                      a.ctrl->tile_ctr + p, &a.ctrl->error_word, s));
         }
+    }
+    NXB_TRY(launch_bvh8_batch_init(a.pairs, a.slots, mb, a.ctr8, a.mesh_nodes, a.mesh_leaves, g, s));
+    if (a.total > 0) {
         const bool in_a = (plan.passes % 2) == 0;
         uint64_t* keys = in_a ? a.keys_a : a.keys_b;
         uint32_t* perm = in_a ? a.vals_a : a.vals_b;
         uint32_t* tokens = in_a ? a.vals_b : a.vals_a;
-        if (fused) {
-            // the collapse starts on the side stream and takes each mesh's
-            // root item as H-PLOC publishes it
-            NXB_TRY(launch_bvh8_batch_init(a.pairs, a.slots, mb, a.ctr8, a.mesh_nodes, a.mesh_leaves, true, s));
-            NXB_TRY(cudaEventRecord(fork->fork, s));
-            NXB_TRY(cudaStreamWaitEvent(fork->side, fork->fork, 0));
-            NXB_TRY(launch_bvh8_batch(a.bvh2, mb, a.total, a.bvh8, a.slots, a.prim_idx, a.pairs, a.ctr8,
-                                      a.mesh_nodes, a.mesh_leaves, &a.ctrl->error_word, t.auction, true, fork->side));
-            NXB_TRY(cudaEventRecord(fork->join, fork->side));
+        // H-PLOC group by group on s; the collapse of group k follows it on
+        // the side stream (ordered by an event, no wait inside any kernel),
+        // overlapping H-PLOC of group k+1
+        for (uint32_t k = 0; k < g.count; ++k) {
+            NXB_TRY(launch_hploc_batch(keys, perm, a.parent, a.bvh2, mb, g.prim[k], g.prim[k + 1], t.radius, tokens,
+                                       a.pol, a.ctrl->leaf_ctr + k, &a.ctrl->error_word, t.hploc_ctas_per_sm, s));
+            const uint32_t m0 = g.mesh[k];
+            const MeshBatch view{a.off + m0, a.off8 + m0, g.mesh[k + 1] - m0};
+            cudaStream_t bs = s;
+            if (g.count > 1) {
+                NXB_TRY(cudaEventRecord(fork->hploc[k], s));
+                NXB_TRY(cudaStreamWaitEvent(fork->side, fork->hploc[k], 0));
+                bs = fork->side;
+            }
+            NXB_TRY(launch_bvh8_batch(a.bvh2, view, g.prim[k + 1] - g.prim[k], a.bvh8, g.slot[k + 1] - g.slot[k],
+                                      a.prim_idx, a.pairs + g.slot[k], a.ctr8 + k * kBvh8CtrWords,
+                                      a.mesh_nodes + m0, a.mesh_leaves + m0, &a.ctrl->error_word, t.auction, bs));
         }
-        NXB_TRY(launch_hploc_batch(keys, perm, a.parent, a.bvh2, mb, a.total, t.radius, tokens, a.pol,
-                                   &a.ctrl->leaf_ctr, &a.ctrl->error_word, t.hploc_ctas_per_sm,
-                                   fused ? a.pairs : nullptr, s));
-    }
-    if (fused) {
-        NXB_TRY(cudaStreamWaitEvent(s, fork->join, 0));
-    } else {
-        NXB_TRY(launch_bvh8_batch_init(a.pairs, a.slots, mb, a.ctr8, a.mesh_nodes, a.mesh_leaves, false, s));
-        if (a.total > 0)
-            NXB_TRY(launch_bvh8_batch(a.bvh2, mb, a.total, a.bvh8, a.slots, a.prim_idx, a.pairs, a.ctr8,
-                                      a.mesh_nodes, a.mesh_leaves, &a.ctrl->error_word, t.auction, false, s));
+        if (g.count > 1) {
+            NXB_TRY(cudaEventRecord(fork->join, fork->side));
+            NXB_TRY(cudaStreamWaitEvent(s, fork->join, 0));
+        }
     }
     NXB_TRY(launch_batch_finalize(mb, a.scene_ord, a.mesh_nodes, a.mesh_leaves, a.results, s));
     if (h_err)
@@ -194,7 +221,10 @@ struct nxb_batch {
     unsigned char* mem = nullptr;
     uint32_t* h_err = nullptr;  // pinned; the graph copies the error word here
     cudaStream_t cap_stream = nullptr;
-    BatchFork fork{nullptr, nullptr, nullptr};  // side stream of a fused capture
+    BatchFork fork{};               // side stream and events of a grouped capture
+    std::vector<uint32_t> h_off;    // host copies of the offsets (mesh groups)
+    std::vector<uint32_t> h_off8;
+    MeshGroups groups{};            // of the current tuning
     cudaGraphExec_t exec = nullptr;
     const void* graph_prims = nullptr;
     bool graph_valid = false;
@@ -214,15 +244,16 @@ BatchTuning tuning_of(const nxb_batch_tuning& t, bool auction) {
     r.digit_bits = t.sort_digit_bits;
     r.radius = t.search_radius;
     r.hploc_ctas_per_sm = t.hploc_ctas_per_sm;
-    r.fuse = t.fuse_bvh8 != 0;
+    r.groups = t.fusion_groups ? t.fusion_groups : 1u;
+    r.block = t.block_size ? t.block_size : 256u;
     return r;
 }
 
 nxb_status capture(nxb_batch* b, const void* prims) {
     cudaGraph_t g = nullptr;
     NXB_TRY(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeRelaxed));
-    const nxb_status st =
-        batch_enqueue(b->arena, prims, b->type, tuning_of(b->tuning, b->auction), b->h_err, b->cap_stream, &b->fork);
+    const nxb_status st = batch_enqueue(b->arena, prims, b->type, tuning_of(b->tuning, b->auction), b->h_err,
+                                        b->cap_stream, &b->groups, &b->fork);
     const cudaError_t ec = cudaStreamEndCapture(b->cap_stream, &g);
     if (st != NXB_OK) {
         if (g) cudaGraphDestroy(g);
@@ -250,7 +281,8 @@ void release(nxb_batch* b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
     if (b->fork.side) cudaStreamDestroy(b->fork.side);
-    if (b->fork.fork) cudaEventDestroy(b->fork.fork);
+    for (cudaEvent_t ev : b->fork.hploc)
+        if (ev) cudaEventDestroy(ev);
     if (b->fork.join) cudaEventDestroy(b->fork.join);
     if (b->h_err) cudaFreeHost(b->h_err);
     if (b->mem) cudaFree(b->mem);
@@ -284,11 +316,17 @@ nxb_status nxb_batch_create(nxb_prim_type type, const uint32_t* h_off, uint32_t 
     b->tuning.sort_digit_bits = 8;
     b->tuning.search_radius = radius;
     b->tuning.hploc_ctas_per_sm = 0;
+    b->tuning.fusion_groups = 1;
+    b->tuning.block_size = 256;
+    b->h_off.assign(h_off, h_off + meshes + 1);
+    b->h_off8 = off8;
+    batch_groups(h_off, off8.data(), meshes, 1, &b->groups);
     cudaError_t e = cudaMalloc(&b->mem, b->arena.bytes);
     if (!e) e = cudaMallocHost(&b->h_err, sizeof(uint32_t));
     if (!e) e = cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking);
     if (!e) e = cudaStreamCreateWithFlags(&b->fork.side, cudaStreamNonBlocking);
-    if (!e) e = cudaEventCreateWithFlags(&b->fork.fork, cudaEventDisableTiming);
+    for (uint32_t k = 0; k < kMaxMeshGroups && !e; ++k)
+        e = cudaEventCreateWithFlags(&b->fork.hploc[k], cudaEventDisableTiming);
     if (!e) e = cudaEventCreateWithFlags(&b->fork.join, cudaEventDisableTiming);
     if (!e) {
         batch_bind(b->mem, &b->arena);
@@ -356,10 +394,15 @@ nxb_status nxb_batch_set_tuning(nxb_batch* b, const nxb_batch_tuning* t) {
     if (!b || !t) return NXB_ERR_INVALID_ARGUMENT;
     if (!batch_digit_ok(b->arena.mesh_bits, t->sort_digit_bits)) return NXB_ERR_UNSUPPORTED;
     if (t->search_radius != 4 && t->search_radius != 8 && t->search_radius != 16) return NXB_ERR_UNSUPPORTED;
+    if (t->block_size != 0 && t->block_size != 128 && t->block_size != 256 && t->block_size != 512)
+        return NXB_ERR_UNSUPPORTED;
+    if (t->fusion_groups > kMaxMeshGroups) return NXB_ERR_UNSUPPORTED;
     b->tuning.sort_digit_bits = t->sort_digit_bits;
     b->tuning.search_radius = t->search_radius;
     b->tuning.hploc_ctas_per_sm = t->hploc_ctas_per_sm;
-    b->tuning.fuse_bvh8 = t->fuse_bvh8 ? 1u : 0u;
+    b->tuning.fusion_groups = t->fusion_groups ? t->fusion_groups : 1u;
+    b->tuning.block_size = t->block_size ? t->block_size : 256u;
+    batch_groups(b->h_off.data(), b->h_off8.data(), b->arena.meshes, b->tuning.fusion_groups, &b->groups);
     b->graph_valid = false;
     return NXB_OK;
 }
@@ -380,9 +423,25 @@ nxb_status nxb_batch_autotune(nxb_batch* b, const void* prims, uint32_t flags, u
         radii = {4, 8, 16};
     else
         radii = {b->tuning.search_radius};
-    const uint32_t digits[] = {8, 7, 6, 5};
-    const uint32_t ctas[] = {0, 4};
-    const uint32_t fuses[] = {0, 1};
+    // candidates: every combination of the knobs that keep each tree as it
+    // is (and the radius, when asked for)
+    const nxb_batch_tuning start = b->tuning;
+    std::vector<nxb_batch_tuning> cand;
+    for (uint32_t r : radii)
+        for (uint32_t d : {8u, 7u, 6u, 5u}) {
+            if (!batch_digit_ok(b->arena.mesh_bits, d)) continue;
+            for (uint32_t c : {0u, 4u})
+                for (uint32_t g : {1u, 2u, 4u})
+                    for (uint32_t bs : {256u, 128u, 512u}) {
+                        nxb_batch_tuning t = start;
+                        t.search_radius = r;
+                        t.sort_digit_bits = d;
+                        t.hploc_ctas_per_sm = c;
+                        t.fusion_groups = g;
+                        t.block_size = bs;
+                        cand.push_back(t);
+                    }
+        }
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     NXB_TRY(cudaEventCreate(&e0));
     const cudaError_t ce = cudaEventCreate(&e1);
@@ -390,42 +449,28 @@ nxb_status nxb_batch_autotune(nxb_batch* b, const void* prims, uint32_t flags, u
         cudaEventDestroy(e0);
         return record_cuda_error(ce);
     }
-    const nxb_batch_tuning start = b->tuning;
     nxb_batch_tuning best = start;
     best.build_ms = 3.4e38f;
     uint32_t tried = 0;
     nxb_status st = NXB_OK;
-    for (uint32_t r : radii) {
-        for (uint32_t d : digits) {
-            if (!batch_digit_ok(b->arena.mesh_bits, d)) continue;
-            for (uint32_t c : ctas)
-            for (uint32_t f : fuses) {
-                nxb_batch_tuning t = start;
-                t.sort_digit_bits = d;
-                t.search_radius = r;
-                t.hploc_ctas_per_sm = c;
-                t.fuse_bvh8 = f;
-                if ((st = nxb_batch_set_tuning(b, &t)) != NXB_OK) break;
-                if ((st = nxb_batch_build(b, prims, s, nullptr)) != NXB_OK) break;  // capture + warm-up
-                std::vector<float> ms;
-                for (uint32_t k = 0; k < repeats && st == NXB_OK; ++k) {
-                    cudaEventRecord(e0, s);
-                    st = nxb_batch_build_async(b, prims, s);
-                    cudaEventRecord(e1, s);
-                    if (st == NXB_OK) st = nxb_batch_wait(b, s, nullptr);
-                    float t_ms = 0.f;
-                    cudaEventElapsedTime(&t_ms, e0, e1);
-                    ms.push_back(t_ms);
-                }
-                if (st != NXB_OK) break;
-                std::sort(ms.begin(), ms.end());
-                t.build_ms = ms[ms.size() / 2];
-                ++tried;
-                if (t.build_ms < best.build_ms) best = t;
-            }
-            if (st != NXB_OK) break;
+    for (nxb_batch_tuning t : cand) {
+        if ((st = nxb_batch_set_tuning(b, &t)) != NXB_OK) break;
+        if ((st = nxb_batch_build(b, prims, s, nullptr)) != NXB_OK) break;  // capture + warm-up
+        std::vector<float> ms;
+        for (uint32_t k = 0; k < repeats && st == NXB_OK; ++k) {
+            cudaEventRecord(e0, s);
+            st = nxb_batch_build_async(b, prims, s);
+            cudaEventRecord(e1, s);
+            if (st == NXB_OK) st = nxb_batch_wait(b, s, nullptr);
+            float t_ms = 0.f;
+            cudaEventElapsedTime(&t_ms, e0, e1);
+            ms.push_back(t_ms);
         }
         if (st != NXB_OK) break;
+        std::sort(ms.begin(), ms.end());
+        t.build_ms = ms[ms.size() / 2];
+        ++tried;
+        if (t.build_ms < best.build_ms) best = t;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

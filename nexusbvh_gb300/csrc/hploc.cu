@@ -84,8 +84,6 @@ struct MergeCtx {
     uint32_t n;
     uint32_t node_limit;       // 2n-1
     uint32_t* err;
-    uint64_t* publish;         // batched, BVH8 running alongside: the mesh's BVH8 root item slot
-    uint64_t item;             // ... and the item written there once the root is stored
 };
 
 // One round of PLOC merging (MergeClustersCreateBVH2Node,
@@ -183,10 +181,8 @@ __device__ __forceinline__ MergeCtx mesh_ctx(const MergeCtx& all, const Seg& seg
         const uint32_t mesh = __shfl_sync(kFullMask, me.m, owner);
         start = __shfl_sync(kFullMask, me.start, owner);
         const uint32_t count = __shfl_sync(kFullMask, me.count, owner);
-        uint64_t* pub = all.publish ? all.publish + mesh : nullptr;
-        const uint64_t item = pub ? ((uint64_t)(2 * count - 2) << 32) | __ldg(seg.off8 + mesh) : 0ull;
         return MergeCtx{all.nodes + 2ull * start, all.tok, all.parent_of_last + mesh, count, 2 * count - 1, all.err,
-                        pub, item};
+};
     } else {
         start = 0;
         return all;
@@ -251,11 +247,6 @@ __device__ __forceinline__ void merge_windows(uint32_t owner, uint32_t left, uin
     while (num > threshold) {
         if (fin && num == 2) {
             merge_root(m, cid, ctok, cb);
-            if (m.publish && lane == 0) {
-                // the tree is complete: hand its root to the BVH8 collapse
-                fence_acq_rel_gpu();
-                st_relaxed_u64(m.publish, m.item);
-            }
             num = 1;
             break;
         }
@@ -301,11 +292,11 @@ constexpr uint32_t kLeafChunk = 256;
 
 template <typename K, int R, typename Seg>
 __global__ __launch_bounds__(kThreads, 12) void hploc_kernel(const K* __restrict__ keys, uint32_t* cluster,
-                                                         uint32_t* parent, Node2* nodes, Seg seg, uint32_t total,
+                                                         uint32_t* parent, Node2* nodes, Seg seg, uint32_t begin,
                                                          uint32_t* tok, uint32_t* parent_of_last, uint32_t* leaf_ctr,
-                                                         uint32_t* err, uint64_t* publish) {
+                                                         uint32_t* err, uint32_t end) {
     const uint32_t lane = lane_id();
-    const MergeCtx all{nodes, tok, parent_of_last, total, 2 * total - 1, err, publish, 0ull};
+    const MergeCtx all{nodes, tok, parent_of_last, end, 2 * end - 1, err};
     uint32_t left = 0, right = 0, split = 0;
     // the lane's mesh; a plain build has one, known at compile time
     MeshSpan me = Seg::kBatch ? MeshSpan{0, 0, 0} : seg.of_prim(0);
@@ -318,14 +309,14 @@ __global__ __launch_bounds__(kThreads, 12) void hploc_kernel(const K* __restrict
         while (need && !exhausted) {
             if (chunk_next == chunk_end) {
                 uint32_t b = 0;
-                if (lane == 0) b = atomicAdd(leaf_ctr, kLeafChunk);
+                if (lane == 0) b = begin + atomicAdd(leaf_ctr, kLeafChunk);
                 b = __shfl_sync(kFullMask, b, 0);
-                if (b >= total) {
+                if (b >= end) {
                     exhausted = true;
                     break;
                 }
                 chunk_next = b;
-                chunk_end = min(b + kLeafChunk, total);
+                chunk_end = min(b + kLeafChunk, end);
             }
             const uint32_t avail = chunk_end - chunk_next;
             const uint32_t rank = __popc(need & lanemask_lt());
@@ -378,34 +369,34 @@ __global__ __launch_bounds__(kThreads, 12) void hploc_kernel(const K* __restrict
 }
 
 template <typename K, int R, typename Seg>
-cudaError_t launch_r(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, Seg seg, uint32_t total,
-                     uint32_t* tok, uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err, uint32_t max_per_sm,
-                     uint64_t* publish, cudaStream_t s) {
+cudaError_t launch_r(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, Seg seg, uint32_t begin,
+                     uint32_t end, uint32_t* tok, uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err,
+                     uint32_t max_per_sm, cudaStream_t s) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hploc_kernel<K, R, Seg>, kThreads, 0);
     if (max_per_sm && (uint32_t)per_sm > max_per_sm) per_sm = (int)max_per_sm;
     if (per_sm < 1) per_sm = 1;
-    const uint32_t want = (total + kThreads - 1) / kThreads;
+    const uint32_t want = (end - begin + kThreads - 1) / kThreads;
     const uint32_t grid = std::max(1u, std::min(want, (uint32_t)(device_info().sms * per_sm)));
-    hploc_kernel<K, R, Seg><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, seg, total, tok, pol, leaf_ctr,
-                                                      err, publish);
+    hploc_kernel<K, R, Seg><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, seg, begin, tok, pol, leaf_ctr,
+                                                      err, end);
     return cudaGetLastError();
 }
 
 template <typename K, typename Seg>
-cudaError_t launch_t(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, Seg seg, uint32_t total,
-                     uint32_t radius, uint32_t* tok, uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err,
-                     uint32_t max_per_sm, uint64_t* publish, cudaStream_t s) {
+cudaError_t launch_t(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, Seg seg, uint32_t begin,
+                     uint32_t end, uint32_t radius, uint32_t* tok, uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err,
+                     uint32_t max_per_sm, cudaStream_t s) {
     switch (radius) {
         case 4:
-            return launch_r<K, 4>(keys, cluster, parent, nodes, seg, total, tok, pol, leaf_ctr, err, max_per_sm,
-                                  publish, s);
+            return launch_r<K, 4>(keys, cluster, parent, nodes, seg, begin, end, tok, pol, leaf_ctr, err, max_per_sm,
+                                  s);
         case 16:
-            return launch_r<K, 16>(keys, cluster, parent, nodes, seg, total, tok, pol, leaf_ctr, err, max_per_sm,
-                                   publish, s);
+            return launch_r<K, 16>(keys, cluster, parent, nodes, seg, begin, end, tok, pol, leaf_ctr, err,
+                                   max_per_sm, s);
         default:
-            return launch_r<K, 8>(keys, cluster, parent, nodes, seg, total, tok, pol, leaf_ctr, err, max_per_sm,
-                                  publish, s);
+            return launch_r<K, 8>(keys, cluster, parent, nodes, seg, begin, end, tok, pol, leaf_ctr, err, max_per_sm,
+                                  s);
     }
 }
 
@@ -416,18 +407,18 @@ cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster
                          uint32_t* err, cudaStream_t s) {
     const SingleMesh seg{n};
     if (key_bytes == 4)
-        return launch_t((const uint32_t*)keys, cluster_idx, parent, nodes, seg, n, radius, tokens, parent_of_last,
-                        leaf_ctr, err, 0u, nullptr, s);
-    return launch_t((const uint64_t*)keys, cluster_idx, parent, nodes, seg, n, radius, tokens, parent_of_last,
-                    leaf_ctr, err, 0u, nullptr, s);
+        return launch_t((const uint32_t*)keys, cluster_idx, parent, nodes, seg, 0u, n, radius, tokens,
+                        parent_of_last, leaf_ctr, err, 0u, s);
+    return launch_t((const uint64_t*)keys, cluster_idx, parent, nodes, seg, 0u, n, radius, tokens, parent_of_last,
+                    leaf_ctr, err, 0u, s);
 }
 
 cudaError_t launch_hploc_batch(const uint64_t* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
-                               const MeshBatch& batch, uint32_t total, uint32_t radius, uint32_t* tokens,
-                               uint32_t* parent_of_last, uint32_t* leaf_ctr, uint32_t* err, uint32_t ctas_per_sm,
-                               uint64_t* publish, cudaStream_t s) {
-    return launch_t(reinterpret_cast<const MeshKey*>(keys), cluster_idx, parent, nodes, batch, total, radius, tokens,
-                    parent_of_last, leaf_ctr, err, ctas_per_sm, publish, s);
+                               const MeshBatch& batch, uint32_t begin, uint32_t end, uint32_t radius,
+                               uint32_t* tokens, uint32_t* parent_of_last, uint32_t* leaf_ctr, uint32_t* err,
+                               uint32_t ctas_per_sm, cudaStream_t s) {
+    return launch_t(reinterpret_cast<const MeshKey*>(keys), cluster_idx, parent, nodes, batch, begin, end, radius,
+                    tokens, parent_of_last, leaf_ctr, err, ctas_per_sm, s);
 }
 
 }  // namespace nxb

@@ -111,29 +111,43 @@ cudaError_t launch_bvh8(const Node2* bvh2, uint32_t n, Node8* out, uint32_t cap,
 // The same stages over independent meshes laid end to end (MeshBatch in
 // common.cuh): one launch per stage for the whole batch.
 // scene_ord: 6 words per mesh, zero on entry.
+// block: CTA size of the two tile kernels (128, 256 or 512).
 cudaError_t launch_batch_bounds(const void* prims, int prim_type, const MeshBatch& batch, uint32_t total,
-                                Node2* nodes, uint32_t* scene_ord, cudaStream_t s);
+                                Node2* nodes, uint32_t* scene_ord, uint32_t block, cudaStream_t s);
 // keys: mesh << 32 | 30-bit code; vals: mesh-local primitive index; hist:
 // kMaxSortPasses x kRadixBins words, zero on entry.
 cudaError_t launch_batch_morton(const Node2* nodes, const MeshBatch& batch, uint32_t total, const uint32_t* scene_ord,
                                 uint64_t* keys, uint32_t* vals, const SortPlan& plan, uint32_t* hist,
-                                const MortonFused& fill, cudaStream_t s);
-// parent_of_last: one word per mesh holding INVALID on entry; ctas_per_sm
-// caps the persistent grid (0: as many CTAs as fit).  publish (optional):
-// BVH8 item slots, one per mesh; when a mesh's root is stored, its BVH8 root
-// item is written to publish[mesh] (the BVH8 collapse runs alongside).
+                                const MortonFused& fill, uint32_t block, cudaStream_t s);
+// H-PLOC over the sorted positions [begin, end), which must cover whole
+// meshes; leaf_ctr: a zeroed word of its own.  parent_of_last: one word per
+// mesh holding INVALID on entry; ctas_per_sm caps the persistent grid (0: as
+// many CTAs as fit).
 cudaError_t launch_hploc_batch(const uint64_t* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
-                               const MeshBatch& batch, uint32_t total, uint32_t radius, uint32_t* tokens,
-                               uint32_t* parent_of_last, uint32_t* leaf_ctr, uint32_t* err, uint32_t ctas_per_sm,
-                               uint64_t* publish, cudaStream_t s);
-// pairs: `slots` = off8[meshes] uint64 slots; ctr: kBvh8CtrWords words.
-// fused: the root items of meshes of 2+ primitives are left for H-PLOC to
-// publish, and the collapse runs while H-PLOC still builds other meshes.
+                               const MeshBatch& batch, uint32_t begin, uint32_t end, uint32_t radius,
+                               uint32_t* tokens, uint32_t* parent_of_last, uint32_t* leaf_ctr, uint32_t* err,
+                               uint32_t ctas_per_sm, cudaStream_t s);
+// Meshes cut into consecutive groups whose BVH8 collapses are separate
+// launches: group g holds meshes [mesh[g], mesh[g+1]), primitives
+// [prim[g], prim[g+1]) and BVH8 slots [slot[g], slot[g+1]).
+constexpr uint32_t kMaxMeshGroups = 8;
+struct MeshGroups {
+    uint32_t count;
+    uint32_t mesh[kMaxMeshGroups + 1];
+    uint32_t prim[kMaxMeshGroups + 1];
+    uint32_t slot[kMaxMeshGroups + 1];
+};
+// pairs: `slots` = off8[meshes] uint64 slots; ctr: kBvh8CtrWords words per
+// group.  Seeds every group's queue with the root items of its meshes.
 cudaError_t launch_bvh8_batch_init(uint64_t* pairs, uint32_t slots, const MeshBatch& batch, uint32_t* ctr,
-                                   uint32_t* mesh_nodes, uint32_t* mesh_leaves, bool fused, cudaStream_t s);
+                                   uint32_t* mesh_nodes, uint32_t* mesh_leaves, const MeshGroups& groups,
+                                   cudaStream_t s);
+// The collapse of the meshes of `batch` (a whole batch, or one group's view:
+// off, off8, mesh_nodes and mesh_leaves advanced to the group's first mesh,
+// pairs to its first slot, ctr to its counters).
 cudaError_t launch_bvh8_batch(const Node2* bvh2, const MeshBatch& batch, uint32_t total, Node8* out, uint32_t slots,
                               uint32_t* prim_idx, uint64_t* pairs, uint32_t* ctr, uint32_t* mesh_nodes,
-                              uint32_t* mesh_leaves, uint32_t* err, bool auction, bool fused, cudaStream_t s);
+                              uint32_t* mesh_leaves, uint32_t* err, bool auction, cudaStream_t s);
 cudaError_t launch_batch_finalize(const MeshBatch& batch, const uint32_t* scene_ord, const uint32_t* mesh_nodes,
                                   const uint32_t* mesh_leaves, nxb_batch_mesh* out, cudaStream_t s);
 // One batched build's device memory (a single allocation carved into
@@ -141,8 +155,9 @@ cudaError_t launch_batch_finalize(const MeshBatch& batch, const uint32_t* scene_
 // the BVH8 offsets; results receives one nxb_batch_mesh per mesh.
 struct BatchCtrl {
     uint32_t error_word;
-    uint32_t leaf_ctr;
-    uint32_t pad[30];
+    uint32_t pad[31];
+    uint32_t leaf_ctr[kMaxMeshGroups];  // one H-PLOC leaf counter per mesh group
+    uint32_t pad2[32 - kMaxMeshGroups];
     uint32_t tile_ctr[kMaxSortPasses];
     uint32_t hist[kMaxSortPasses][kRadixBins];
 };
@@ -176,13 +191,16 @@ struct BatchArena {
 struct BatchTuning {
     uint32_t digit_bits = 8, radius = 8, hploc_ctas_per_sm = 0;
     bool auction = false;
-    bool fuse = false;  // BVH8 collapse alongside H-PLOC (needs a BatchFork)
+    uint32_t groups = 1;   // BVH2/BVH8 fusion point: mesh groups (needs a BatchFork when > 1)
+    uint32_t block = 256;  // CTA size of the bounds and Morton tile kernels
 };
-// A second stream and two events for running the BVH8 collapse alongside
-// H-PLOC (BatchTuning::fuse).
+// A second stream and two events per mesh group: the BVH8 collapse of group
+// g runs on `side` after H-PLOC of group g (event hploc[g]) while H-PLOC of
+// group g+1 runs on the main stream; `join` brings the side stream back.
 struct BatchFork {
     cudaStream_t side;
-    cudaEvent_t fork, join;
+    cudaEvent_t hploc[kMaxMeshGroups];
+    cudaEvent_t join;
 };
 // BVH8 node capacity of one mesh (the reference's ceil((4n-1)/7); 1 for an
 // empty mesh, so that BVH8 offsets are strictly increasing).
@@ -193,12 +211,17 @@ uint32_t batch_bvh8_capacity(uint32_t n);
 bool batch_layout(const uint32_t* h_off, uint32_t meshes, uint32_t* h_off8, BatchArena* a);
 void batch_bind(unsigned char* base, BatchArena* a);
 bool batch_digit_ok(uint32_t mesh_bits, uint32_t digit_bits);
+// Cuts meshes [0, meshes) with host offsets h_off / h_off8 into at most
+// `want` groups of about equal primitive counts (never an empty group).
+void batch_groups(const uint32_t* h_off, const uint32_t* h_off8, uint32_t meshes, uint32_t want, MeshGroups* g);
 // The batched pipeline on stream s; off/off8 must already be on the device.
 // If h_err is not null, the error word is copied there at the end.  With
-// t.fuse and a fork, the BVH8 collapse runs on fork->side alongside H-PLOC
-// (joined back into s before the end).
+// groups (count > 1) and a fork, H-PLOC runs group by group on s and the
+// collapse of each group follows on fork->side, overlapping H-PLOC of the
+// next group; without, the whole batch is one group.
 nxb_status batch_enqueue(const BatchArena& a, const void* prims, nxb_prim_type type, const BatchTuning& t,
-                         uint32_t* h_err, cudaStream_t s, const BatchFork* fork = nullptr);
+                         uint32_t* h_err, cudaStream_t s, const MeshGroups* groups = nullptr,
+                         const BatchFork* fork = nullptr);
 // ---------------------------------------------------------------- eval
 cudaError_t launch_bvh2_cost(const Node2* nodes, uint32_t count, const nxb_aabb* root, float* cost, cudaStream_t s);
 cudaError_t launch_bvh8_cost(const Node8* nodes, uint32_t count, const nxb_aabb* root, float* cost, cudaStream_t s);

@@ -281,29 +281,29 @@ __device__ __forceinline__ void warp_reduce_box(Box& b) {
 // tile inside one mesh reduces its box over the CTA into one set of 6
 // atomics on scene_ord[6m .. 6m+5]; a tile that spans meshes (about one per
 // mesh boundary) reduces per warp, or per lane where a warp spans meshes.
-template <int FLOATS>
-__global__ __launch_bounds__(kThreads) void batch_bounds_kernel(const float* __restrict__ prims, MeshBatch batch,
+template <int FLOATS, int T>
+__global__ __launch_bounds__(T) void batch_bounds_kernel(const float* __restrict__ prims, MeshBatch batch,
                                                                 uint32_t total, Node2* __restrict__ nodes,
                                                                 uint32_t* scene_ord, bool aligned16) {
-    __shared__ __align__(16) float tile[kThreads * FLOATS];
+    __shared__ __align__(16) float tile[T * FLOATS];
     __shared__ uint32_t s_rng[2];
-    __shared__ float s_red[kThreads / 32][6];
-    const uint32_t tiles = (total + kThreads - 1) / kThreads;
+    __shared__ float s_red[T / 32][6];
+    const uint32_t tiles = (total + T - 1) / T;
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
     for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x) {
-        const uint32_t first = t * kThreads;
-        const uint32_t cnt = min((uint32_t)kThreads, total - first);
+        const uint32_t first = t * T;
+        const uint32_t cnt = min((uint32_t)T, total - first);
         const float* src = prims + (size_t)first * FLOATS;
         __syncthreads();
         if (threadIdx.x == 0) tile_meshes(batch, first, first + cnt - 1, s_rng);
-        if (cnt == kThreads && aligned16) {
-            constexpr int V = kThreads * FLOATS / 4;
+        if (cnt == T && aligned16) {
+            constexpr int V = T * FLOATS / 4;
             const float4* s4 = reinterpret_cast<const float4*>(src);
             float4* d4 = reinterpret_cast<float4*>(tile);
 #pragma unroll
-            for (int v = threadIdx.x; v < V; v += kThreads) d4[v] = __ldcs(s4 + v);
+            for (int v = threadIdx.x; v < V; v += T) d4[v] = __ldcs(s4 + v);
         } else {
-            for (uint32_t v = threadIdx.x; v < cnt * FLOATS; v += kThreads) tile[v] = __ldcs(src + v);
+            for (uint32_t v = threadIdx.x; v < cnt * FLOATS; v += T) tile[v] = __ldcs(src + v);
         }
         __syncthreads();
         const uint32_t lo = s_rng[0], hi = s_rng[1];
@@ -342,7 +342,7 @@ __global__ __launch_bounds__(kThreads) void batch_bounds_kernel(const float* __r
             if (threadIdx.x < 6) {
                 const int a = threadIdx.x;
                 float v = s_red[0][a];
-                for (int w = 1; w < kThreads / 32; ++w) v = a < 3 ? fminf(v, s_red[w][a]) : fmaxf(v, s_red[w][a]);
+                for (int w = 1; w < T / 32; ++w) v = a < 3 ? fminf(v, s_red[w][a]) : fmaxf(v, s_red[w][a]);
                 atomicMax(scene_ord + 6ull * lo + a, a < 3 ? ~f2ord(v) : f2ord(v));
             }
         } else {
@@ -363,8 +363,8 @@ __global__ __launch_bounds__(kThreads) void batch_bounds_kernel(const float* __r
 // kernel, and the same fill work (parent slots, look-back flags).  Tiles of
 // 256 elements: a tile inside one mesh reads the mesh's span and scene box
 // once, into shared memory.
-template <bool HIST>
-__global__ __launch_bounds__(kThreads) void batch_morton_kernel(const Node2* __restrict__ nodes, MeshBatch batch,
+template <bool HIST, int T>
+__global__ __launch_bounds__(T) void batch_morton_kernel(const Node2* __restrict__ nodes, MeshBatch batch,
                                                                 uint32_t total, const uint32_t* scene_ord,
                                                                 uint64_t* __restrict__ keys, uint32_t* vals,
                                                                 uint32_t* hist, MortonArgs a) {
@@ -372,12 +372,12 @@ __global__ __launch_bounds__(kThreads) void batch_morton_kernel(const Node2* __r
     __shared__ uint32_t s_rng[2];
     __shared__ float s_scene[6];
     if (HIST)
-        for (int i = threadIdx.x; i < a.pd.passes * kRadixBins; i += kThreads) s_hist[i] = 0;
-    const uint32_t tiles = (total + kThreads - 1) / kThreads;
-    const uint32_t stride = gridDim.x * kThreads;
+        for (int i = threadIdx.x; i < a.pd.passes * kRadixBins; i += T) s_hist[i] = 0;
+    const uint32_t tiles = (total + T - 1) / T;
+    const uint32_t stride = gridDim.x * T;
     for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x) {
-        const uint32_t first = t * kThreads;
-        const uint32_t cnt = min((uint32_t)kThreads, total - first);
+        const uint32_t first = t * T;
+        const uint32_t cnt = min((uint32_t)T, total - first);
         __syncthreads();
         if (threadIdx.x == 0) {
             tile_meshes(batch, first, first + cnt - 1, s_rng);
@@ -421,13 +421,13 @@ __global__ __launch_bounds__(kThreads) void batch_morton_kernel(const Node2* __r
             }
         }
     }
-    for (size_t w = (size_t)blockIdx.x * kThreads + threadIdx.x; w < a.zero_vec4; w += stride)
+    for (size_t w = (size_t)blockIdx.x * T + threadIdx.x; w < a.zero_vec4; w += stride)
         a.zero_ptr[w] = make_uint4(0, 0, 0, 0);
-    for (size_t w = (size_t)blockIdx.x * kThreads + threadIdx.x; w < a.ones_vec4; w += stride)
+    for (size_t w = (size_t)blockIdx.x * T + threadIdx.x; w < a.ones_vec4; w += stride)
         a.ones_ptr[w] = make_uint4(kInvalid, kInvalid, kInvalid, kInvalid);
     if (HIST) {
         __syncthreads();
-        for (int i = threadIdx.x; i < a.pd.passes * kRadixBins; i += kThreads)
+        for (int i = threadIdx.x; i < a.pd.passes * kRadixBins; i += T)
             if (s_hist[i]) atomicAdd(hist + i, s_hist[i]);
     }
 }
@@ -533,28 +533,54 @@ cudaError_t launch_sort_histogram(uint32_t key_bytes, const void* keys, uint32_t
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_bounds(const void* prims, int prim_type, const MeshBatch& batch, uint32_t total,
-                                Node2* nodes, uint32_t* scene_ord, cudaStream_t s) {
-    bool aligned = (reinterpret_cast<uintptr_t>(prims) & 15u) == 0;
-    uint32_t grid = grid_for(total, 8);
+template <int T>
+uint32_t batch_grid(uint32_t total) {
+    const uint32_t want = (total + T - 1) / T;
+    const uint32_t cap = (uint32_t)device_info().sms * (2048 / T);
+    return std::max(1u, std::min(want, cap));
+}
+
+template <int T>
+void bounds_t(const void* prims, int prim_type, const MeshBatch& batch, uint32_t total, Node2* nodes,
+              uint32_t* scene_ord, bool aligned, cudaStream_t s) {
     if (prim_type == NXB_PRIM_TRIANGLE)
-        batch_bounds_kernel<9><<<grid, kThreads, 0, s>>>((const float*)prims, batch, total, nodes, scene_ord, aligned);
+        batch_bounds_kernel<9, T><<<batch_grid<T>(total), T, 0, s>>>((const float*)prims, batch, total, nodes,
+                                                                     scene_ord, aligned);
     else
-        batch_bounds_kernel<6><<<grid, kThreads, 0, s>>>((const float*)prims, batch, total, nodes, scene_ord, aligned);
+        batch_bounds_kernel<6, T><<<batch_grid<T>(total), T, 0, s>>>((const float*)prims, batch, total, nodes,
+                                                                     scene_ord, aligned);
+}
+
+cudaError_t launch_batch_bounds(const void* prims, int prim_type, const MeshBatch& batch, uint32_t total,
+                                Node2* nodes, uint32_t* scene_ord, uint32_t block, cudaStream_t s) {
+    const bool aligned = (reinterpret_cast<uintptr_t>(prims) & 15u) == 0;
+    if (block == 128)
+        bounds_t<128>(prims, prim_type, batch, total, nodes, scene_ord, aligned, s);
+    else if (block == 512)
+        bounds_t<512>(prims, prim_type, batch, total, nodes, scene_ord, aligned, s);
+    else
+        bounds_t<256>(prims, prim_type, batch, total, nodes, scene_ord, aligned, s);
     return cudaGetLastError();
 }
 
 cudaError_t launch_batch_morton(const Node2* nodes, const MeshBatch& batch, uint32_t total, const uint32_t* scene_ord,
                                 uint64_t* keys, uint32_t* vals, const SortPlan& plan, uint32_t* hist,
-                                const MortonFused& f, cudaStream_t s) {
+                                const MortonFused& f, uint32_t block, cudaStream_t s) {
     MortonArgs a{};
     a.pd = to_digits(plan);
     a.zero_ptr = reinterpret_cast<uint4*>(f.zero_ptr);
     a.zero_vec4 = f.zero_words / 4;
     a.ones_ptr = reinterpret_cast<uint4*>(f.ones_ptr);
     a.ones_vec4 = f.ones_words / 4;
-    batch_morton_kernel<true><<<grid_for(total, 8), kThreads, 0, s>>>(nodes, batch, total, scene_ord, keys, vals,
-                                                                        hist, a);
+    if (block == 128)
+        batch_morton_kernel<true, 128><<<batch_grid<128>(total), 128, 0, s>>>(nodes, batch, total, scene_ord, keys,
+                                                                              vals, hist, a);
+    else if (block == 512)
+        batch_morton_kernel<true, 512><<<batch_grid<512>(total), 512, 0, s>>>(nodes, batch, total, scene_ord, keys,
+                                                                              vals, hist, a);
+    else
+        batch_morton_kernel<true, 256><<<batch_grid<256>(total), 256, 0, s>>>(nodes, batch, total, scene_ord, keys,
+                                                                              vals, hist, a);
     return cudaGetLastError();
 }
 

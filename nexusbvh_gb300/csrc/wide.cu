@@ -53,13 +53,11 @@ __device__ __forceinline__ uint32_t ceil_log2_biased(float x) {
 }
 __device__ __forceinline__ float inv_pow2(uint8_t e) { return __uint_as_float((uint32_t)(254 - (int)e) << 23); }
 
-// A BVH2 node.  NC: read-only path (the BVH2 was finished by an earlier
-// kernel); otherwise through L2 (the BVH2 is still being written by H-PLOC
-// running alongside, and its nodes become visible through L2).
-template <bool NC = true>
+// A BVH2 node, through the read-only path (the BVH2 was finished by an
+// earlier kernel).
 __device__ __forceinline__ Node2 load_node(const Node2* b2, uint32_t i) {
     const uint4* p = reinterpret_cast<const uint4*>(b2 + i);
-    const uint4 a = NC ? __ldg(p) : __ldcg(p), b = NC ? __ldg(p + 1) : __ldcg(p + 1);
+    const uint4 a = __ldg(p), b = __ldg(p + 1);
     Node2 r;
     r.b.mn = make_float3(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z));
     r.b.mx = make_float3(__uint_as_float(a.w), __uint_as_float(b.x), __uint_as_float(b.y));
@@ -267,26 +265,36 @@ __global__ void bvh8_init_kernel(uint64_t* pairs, uint32_t n, uint32_t* ctr) {
 // Batched form: slot m holds the root item of mesh m (empty meshes too,
 // they finish without output); per-mesh node and leaf counters.
 __global__ void bvh8_batch_init_kernel(uint64_t* pairs, uint32_t slots, MeshBatch batch, uint32_t* ctr,
-                                       uint32_t* mesh_nodes, uint32_t* mesh_leaves, bool fused) {
+                                       uint32_t* mesh_nodes, uint32_t* mesh_leaves, MeshGroups groups) {
     const uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x;
     for (uint32_t i = i0; i < slots; i += gridDim.x * blockDim.x) {
+        // group g's queue is slots [slot[g], slot[g+1]); its first entries
+        // are the root items of the group's meshes
+        uint32_t g = 0;
+        while (g + 1 < groups.count && i >= groups.slot[g + 1]) ++g;
+        const uint32_t local = i - groups.slot[g];
         uint64_t v = ~0ull;
+        if (local < groups.mesh[g + 1] - groups.mesh[g]) {
+            const uint32_t m = groups.mesh[g] + local;
+            const MeshSpan me = batch.span(m);
+            const uint32_t root = me.count ? 2 * me.count - 2 : 0u;
+            v = ((uint64_t)root << 32) | __ldg(batch.off8 + m);
+        }
         if (i < batch.meshes) {
             const MeshSpan me = batch.span(i);
-            const uint32_t root = me.count ? 2 * me.count - 2 : 0u;
-            // fused: H-PLOC publishes the root of a mesh of 2+ primitives
-            if (!fused || me.count <= 1) v = ((uint64_t)root << 32) | __ldg(batch.off8 + i);
             mesh_nodes[i] = me.count ? 1u : 0u;
             mesh_leaves[i] = 0;
         }
         pairs[i] = v;
     }
-    if (i0 == 0) {
-        ctr[kBvh8Claim] = 0;
-        ctr[kBvh8Nodes] = 0;
-        ctr[kBvh8Leaves] = 0;
-        ctr[kBvh8Alloc] = batch.meshes;
-        ctr[kBvh8Pending] = batch.meshes;
+    if (i0 < groups.count) {
+        uint32_t* c = ctr + i0 * kBvh8CtrWords;
+        const uint32_t meshes = groups.mesh[i0 + 1] - groups.mesh[i0];
+        c[kBvh8Claim] = 0;
+        c[kBvh8Nodes] = 0;
+        c[kBvh8Leaves] = 0;
+        c[kBvh8Alloc] = meshes;
+        c[kBvh8Pending] = meshes;
     }
 }
 
@@ -303,7 +311,7 @@ __global__ void bvh8_batch_init_kernel(uint64_t* pairs, uint32_t slots, MeshBatc
 // batched form (Seg = MeshBatch) the items of all meshes share the queue,
 // the BVH8 index names the mesh, and nodes and leaves are counted per mesh
 // in mesh_nodes / mesh_leaves.
-template <typename Seg, bool AUCTION, bool FUSED>
+template <typename Seg, bool AUCTION>
 __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict__ b2, Seg seg, Node8* out,
                                                         uint32_t cap, uint32_t slots, uint32_t* prim_idx,
                                                         uint64_t* pairs, uint32_t* ctr, uint32_t* mesh_nodes,
@@ -357,11 +365,7 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
         uint64_t pr = 0;
         bool ready = false;
         if (slot != kInvalid) {
-            // a root slot of a fused batch is published by H-PLOC: acquire it
-            if constexpr (FUSED)
-                pr = slot < seg.meshes ? ld_acquire_u64(pairs + slot) : ld_relaxed_u64(pairs + slot);
-            else
-                pr = ld_relaxed_u64(pairs + slot);
+            pr = ld_relaxed_u64(pairs + slot);
             ready = (uint32_t)(pr >> 32) != kInvalid;
         }
         if (!__any_sync(kFullMask, ready)) {
@@ -403,7 +407,7 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
             } else if (b2i >= node_limit || b8i - base8 >= cap8) {
                 set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
             } else {
-                nd = load_node<!FUSED>(mb2, b2i);
+                nd = load_node(mb2, b2i);
                 if (nd.left >= node_limit || nd.right >= node_limit)
                     set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
                 else
@@ -418,7 +422,7 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
             uint32_t l0 = nd.left, l1 = nd.right;
             uint32_t msb = 0;
             while (true) {
-                const Node2 c0 = load_node<!FUSED>(mb2, l0), c1 = load_node<!FUSED>(mb2, l1);
+                const Node2 c0 = load_node(mb2, l0), c1 = load_node(mb2, l1);
                 if (kPrefetch) {
                     if (c0.left < node_limit && c0.right < node_limit) {
                         prefetch_l2(mb2 + c0.left);
@@ -527,32 +531,32 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
     }
 }
 
-template <typename Seg, bool AUCTION, bool FUSED>
+template <typename Seg, bool AUCTION>
 cudaError_t configure_smem() {
     static bool configured = false;
     if (configured) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(bvh8_kernel<Seg, AUCTION, FUSED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(bvh8_kernel<Seg, AUCTION>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kSlotSmem);
     if (!e) configured = true;
     return e;
 }
 
-template <typename Seg, bool AUCTION, bool FUSED>
+template <typename Seg, bool AUCTION>
 uint32_t persistent_grid(uint32_t items) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh8_kernel<Seg, AUCTION, FUSED>, kThreads, kSlotSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh8_kernel<Seg, AUCTION>, kThreads, kSlotSmem);
     if (per_sm < 1) per_sm = 1;
     const uint32_t want = (items + kThreads - 1) / kThreads;
     return std::max(1u, std::min(want, (uint32_t)(device_info().sms * per_sm)));
 }
 
-template <typename Seg, bool AUCTION, bool FUSED>
+template <typename Seg, bool AUCTION>
 cudaError_t launch_wide(const Node2* bvh2, Seg seg, uint32_t items, Node8* out, uint32_t cap, uint32_t slots,
                         uint32_t* prim_idx, uint64_t* pairs, uint32_t* ctr, uint32_t* mesh_nodes,
                         uint32_t* mesh_leaves, uint32_t* err, cudaStream_t s) {
-    cudaError_t e = configure_smem<Seg, AUCTION, FUSED>();
+    cudaError_t e = configure_smem<Seg, AUCTION>();
     if (e) return e;
-    bvh8_kernel<Seg, AUCTION, FUSED><<<persistent_grid<Seg, AUCTION, FUSED>(items), kThreads, kSlotSmem, s>>>(
+    bvh8_kernel<Seg, AUCTION><<<persistent_grid<Seg, AUCTION>(items), kThreads, kSlotSmem, s>>>(
         bvh2, seg, out, cap, slots, prim_idx, pairs, ctr, mesh_nodes, mesh_leaves, err);
     return cudaGetLastError();
 }
@@ -565,7 +569,7 @@ cudaError_t run_bvh8_stall_probe(uint32_t* err_out) {
     const uint32_t n = 2;
     unsigned char* buf = nullptr;
     const size_t bytes = 4 * (kBvh8CtrWords + 32) + 3 * sizeof(Node2) + 2 * sizeof(Node8) + 8 * n + 4 * n;
-    cudaError_t e = configure_smem<SingleMesh, false, false>();
+    cudaError_t e = configure_smem<SingleMesh, false>();
     if (!e) e = cudaMalloc(&buf, bytes);
     if (e) return e;
     uint32_t* ctr = (uint32_t*)buf;  // 256-byte aligned
@@ -582,7 +586,7 @@ cudaError_t run_bvh8_stall_probe(uint32_t* err_out) {
     c[kBvh8Pending] = 1;  // ... but its pair is never written
     if (!e) e = cudaMemcpy(ctr, c, sizeof(c), cudaMemcpyHostToDevice);
     if (!e) {
-        bvh8_kernel<SingleMesh, false, false><<<1, kThreads, kSlotSmem>>>(b2, SingleMesh{n}, out, 2, n, prim, pairs, ctr,
+        bvh8_kernel<SingleMesh, false><<<1, kThreads, kSlotSmem>>>(b2, SingleMesh{n}, out, 2, n, prim, pairs, ctr,
                                                                    nullptr, nullptr, err);
         e = cudaGetLastError();
     }
@@ -600,34 +604,28 @@ cudaError_t launch_bvh8_init(uint64_t* pairs, uint32_t n, uint32_t* ctr, cudaStr
 cudaError_t launch_bvh8(const Node2* bvh2, uint32_t n, Node8* out, uint32_t cap, uint32_t* prim_idx, uint64_t* pairs,
                         uint32_t* ctr, uint32_t* err, bool auction, cudaStream_t s) {
     if (auction)
-        return launch_wide<SingleMesh, true, false>(bvh2, SingleMesh{n}, n, out, cap, n, prim_idx, pairs, ctr, nullptr,
+        return launch_wide<SingleMesh, true>(bvh2, SingleMesh{n}, n, out, cap, n, prim_idx, pairs, ctr, nullptr,
                                                     nullptr, err, s);
-    return launch_wide<SingleMesh, false, false>(bvh2, SingleMesh{n}, n, out, cap, n, prim_idx, pairs, ctr, nullptr,
+    return launch_wide<SingleMesh, false>(bvh2, SingleMesh{n}, n, out, cap, n, prim_idx, pairs, ctr, nullptr,
                                                  nullptr, err, s);
 }
 
 cudaError_t launch_bvh8_batch_init(uint64_t* pairs, uint32_t slots, const MeshBatch& batch, uint32_t* ctr,
-                                   uint32_t* mesh_nodes, uint32_t* mesh_leaves, bool fused, cudaStream_t s) {
+                                   uint32_t* mesh_nodes, uint32_t* mesh_leaves, const MeshGroups& groups,
+                                   cudaStream_t s) {
     uint32_t grid = std::max(1u, std::min<uint32_t>((slots + 255) / 256, (uint32_t)device_info().sms * 8));
-    bvh8_batch_init_kernel<<<grid, 256, 0, s>>>(pairs, slots, batch, ctr, mesh_nodes, mesh_leaves, fused);
+    bvh8_batch_init_kernel<<<grid, 256, 0, s>>>(pairs, slots, batch, ctr, mesh_nodes, mesh_leaves, groups);
     return cudaGetLastError();
 }
 
 cudaError_t launch_bvh8_batch(const Node2* bvh2, const MeshBatch& batch, uint32_t total, Node8* out, uint32_t slots,
                               uint32_t* prim_idx, uint64_t* pairs, uint32_t* ctr, uint32_t* mesh_nodes,
-                              uint32_t* mesh_leaves, uint32_t* err, bool auction, bool fused, cudaStream_t s) {
-    if (fused) {
-        if (auction)
-            return launch_wide<MeshBatch, true, true>(bvh2, batch, total, out, 0u, slots, prim_idx, pairs, ctr,
-                                                      mesh_nodes, mesh_leaves, err, s);
-        return launch_wide<MeshBatch, false, true>(bvh2, batch, total, out, 0u, slots, prim_idx, pairs, ctr,
-                                                   mesh_nodes, mesh_leaves, err, s);
-    }
+                              uint32_t* mesh_leaves, uint32_t* err, bool auction, cudaStream_t s) {
     if (auction)
-        return launch_wide<MeshBatch, true, false>(bvh2, batch, total, out, 0u, slots, prim_idx, pairs, ctr,
-                                                   mesh_nodes, mesh_leaves, err, s);
-    return launch_wide<MeshBatch, false, false>(bvh2, batch, total, out, 0u, slots, prim_idx, pairs, ctr, mesh_nodes,
-                                                mesh_leaves, err, s);
+        return launch_wide<MeshBatch, true>(bvh2, batch, total, out, 0u, slots, prim_idx, pairs, ctr, mesh_nodes,
+                                            mesh_leaves, err, s);
+    return launch_wide<MeshBatch, false>(bvh2, batch, total, out, 0u, slots, prim_idx, pairs, ctr, mesh_nodes,
+                                         mesh_leaves, err, s);
 }
 
 }  // namespace nxb

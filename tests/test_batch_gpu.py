@@ -93,18 +93,32 @@ def test_batch_matches_oracle(gpu, orc):
         assert errs8 == 0, rep8
 
 
-def test_batch_fused_collapse_matches_plain_builds(gpu, orc):
-    """BVH2/BVH8 fusion point 1: each mesh's collapse starts when H-PLOC
-    publishes its root, alongside H-PLOC; results equal the plain builds."""
+@pytest.mark.parametrize("groups", [2, 4, 8])
+def test_batch_grouped_collapse_matches_plain_builds(gpu, orc, groups):
+    """BVH2/BVH8 fusion point: meshes cut into groups, the collapse of each
+    group overlapping H-PLOC of the next; results equal the plain builds."""
     prims = make_batch(COUNTS, seed=12)
     batch = nxb.Batch(COUNTS)
     t = batch.tuning()
-    t.fuse_bvh8 = 1
+    t.fusion_groups = groups
     batch.set_tuning(t)
     d = S.dev(prims)
     for _ in range(3):  # capture, then replays
         meshes = batch.build(d)
     check_against_plain(batch, meshes, prims, COUNTS, orc)
+
+
+def test_batch_groups_with_empty_tail(gpu, orc):
+    """A cut that leaves a group of empty meshes only (all triangles in the
+    first mesh) still builds every mesh."""
+    counts = [3000, 0, 0, 1, 0]
+    prims = make_batch(counts, seed=13)
+    batch = nxb.Batch(counts)
+    t = batch.tuning()
+    t.fusion_groups = 4
+    batch.set_tuning(t)
+    meshes = batch.build(S.dev(prims))
+    check_against_plain(batch, meshes, prims, counts, orc)
 
 
 def test_batch_aabb_input(gpu, orc):
@@ -123,9 +137,9 @@ def test_batch_replay_and_tuning_keep_results(gpu, orc):
     first = batch.build(d)
     ref = [(batch.mesh_bvh2_host(m, first).tobytes(), batch.mesh_bvh8_host(m)) for m in range(len(counts))
            if counts[m]]
-    for digits, ctas, fuse in ((5, 0, 0), (6, 4, 1), (7, 0, 1), (8, 4, 0)):
+    for digits, ctas, groups, block in ((5, 0, 1, 128), (6, 4, 2, 512), (7, 0, 4, 256), (8, 4, 1, 512)):
         t = batch.tuning()
-        t.sort_digit_bits, t.hploc_ctas_per_sm, t.fuse_bvh8 = digits, ctas, fuse
+        t.sort_digit_bits, t.hploc_ctas_per_sm, t.fusion_groups, t.block_size = digits, ctas, groups, block
         batch.set_tuning(t)
         for _ in range(2):  # capture, then replay
             again = batch.build(d)
