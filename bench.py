@@ -374,7 +374,8 @@ def run_batch(args, world, rank, local):
         return statistics.median(ms)
 
     chosen = batch.tuning()
-    fusion = {f"groups_{g}_ms": round(timed_build(g), 4) for g in (1, 2, 4, 8)}
+    # the fusion-point sweep is part of the tuning report (skipped with --no-autotune)
+    fusion = None if args.no_autotune else {f"groups_{g}_ms": round(timed_build(g), 4) for g in (1, 2, 4, 8)}
     batch.set_tuning(chosen)
     for _ in range(args.warmup):
         batch.build_async(d_prims)
