@@ -59,7 +59,9 @@ typedef enum nxb_status {
     NXB_ERR_WORKSPACE_TOO_SMALL = 5,
     NXB_ERR_DEVICE_TIMEOUT = 6,   /* a bounded device-side wait gave up (error word set) */
     NXB_ERR_DEVICE_INVARIANT = 7, /* a kernel found an impossible state (error word set) */
-    NXB_ERR_ADMISSION = 8         /* server: the request does not fit the memory budget */
+    NXB_ERR_ADMISSION = 8,        /* server: the request does not fit the memory budget */
+    NXB_ERR_IO = 9                /* a BVH file could not be opened, read or written, or is not
+                                     a BVH file of this format */
 } nxb_status;
 
 /* Returns a static, human-readable name for a status code. */
@@ -170,6 +172,18 @@ nxb_status nxb_bvh8_to_host(const nxb_bvh8* device_bvh, nxb_bvh8* host_bvh);
 nxb_status nxb_free_host_bvh8(nxb_bvh8* host_bvh);
 nxb_status nxb_free_device_bvh2(nxb_bvh2* device_bvh);
 nxb_status nxb_free_device_bvh8(nxb_bvh8* device_bvh);
+
+/* On-disk form of a host BVH (the node layouts of NexusBVH/include/NXB/BVH.h:20-86, which the
+ * reference keeps in memory only).  A file is a 64-byte header -- magic "NXBVH2\0\0" or
+ * "NXBVH8\0\0", format version 1, node count, primitive count, node size in bytes (32 or 80),
+ * root bounds -- then the nodes in their in-memory layout and, for a BVH8, prim_idx; all
+ * little-endian.  Writing takes a host BVH (nxb_bvh*_to_host, or a file read back); reading
+ * fills malloc'd arrays that nxb_free_host_bvh* frees, and checks the magic, the version, the
+ * node size, the counts and the file length, returning NXB_ERR_IO when any is wrong. */
+nxb_status nxb_write_bvh2(const char* path, const nxb_bvh2* host_bvh);
+nxb_status nxb_read_bvh2(const char* path, nxb_bvh2* host_bvh);
+nxb_status nxb_write_bvh8(const char* path, const nxb_bvh8* host_bvh);
+nxb_status nxb_read_bvh8(const char* path, nxb_bvh8* host_bvh);
 
 /* ------------------------------------- allocation-free (workspace) builds */
 /* Sizes, in bytes, of what a build of prim_count primitives needs.  All

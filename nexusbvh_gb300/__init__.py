@@ -31,7 +31,7 @@ INVALID_IDX = 0xFFFFFFFF
 STATUS_NAMES = {
     0: "NXB_OK", 1: "NXB_ERR_INVALID_ARGUMENT", 2: "NXB_ERR_UNSUPPORTED", 3: "NXB_ERR_OUT_OF_MEMORY",
     4: "NXB_ERR_CUDA", 5: "NXB_ERR_WORKSPACE_TOO_SMALL", 6: "NXB_ERR_DEVICE_TIMEOUT",
-    7: "NXB_ERR_DEVICE_INVARIANT", 8: "NXB_ERR_ADMISSION",
+    7: "NXB_ERR_DEVICE_INVARIANT", 8: "NXB_ERR_ADMISSION", 9: "NXB_ERR_IO",
 }
 
 # numpy views of the device layouts
@@ -137,6 +137,10 @@ _SIG = {
     "nxb_bvh8_to_host": (ctypes.c_int, [ctypes.POINTER(CBVH8), ctypes.POINTER(CBVH8)]),
     "nxb_free_host_bvh2": (ctypes.c_int, [ctypes.POINTER(CBVH2)]),
     "nxb_free_host_bvh8": (ctypes.c_int, [ctypes.POINTER(CBVH8)]),
+    "nxb_write_bvh2": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(CBVH2)]),
+    "nxb_read_bvh2": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(CBVH2)]),
+    "nxb_write_bvh8": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(CBVH8)]),
+    "nxb_read_bvh8": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(CBVH8)]),
     "nxb_free_device_bvh2": (ctypes.c_int, [ctypes.POINTER(CBVH2)]),
     "nxb_free_device_bvh8": (ctypes.c_int, [ctypes.POINTER(CBVH8)]),
     "nxb_query_build_sizes": (ctypes.c_int, [_U32, _P, ctypes.POINTER(CSizes)]),
@@ -553,6 +557,54 @@ class Server:
         finally:
             lib.nxb_free_host_bvh8(ctypes.byref(h))
         return nodes, prim
+
+
+def _caabb(bounds) -> CAABB:
+    b = np.asarray(bounds, dtype=np.float32).reshape(2, 3)
+    return CAABB((ctypes.c_float * 3)(*b[0]), (ctypes.c_float * 3)(*b[1]))
+
+
+def save_bvh2(path, nodes: np.ndarray, bounds) -> None:
+    """Writes host BVH2 nodes (BVH2_NODE_DTYPE, 2n-1 of them) and the root
+    bounds ((2, 3): min, max) to a BVH file (nxb_write_bvh2)."""
+    nodes = np.ascontiguousarray(nodes, dtype=BVH2_NODE_DTYPE)
+    h = CBVH2(nodes.ctypes.data, len(nodes), (len(nodes) + 1) // 2, _caabb(bounds))
+    check(load().nxb_write_bvh2(str(path).encode(), ctypes.byref(h)), "nxb_write_bvh2")
+
+
+def load_bvh2(path):
+    """(nodes as BVH2_NODE_DTYPE array, bounds (2, 3)) read from a BVH file."""
+    lib = load()
+    h = CBVH2()
+    check(lib.nxb_read_bvh2(str(path).encode(), ctypes.byref(h)), "nxb_read_bvh2")
+    try:
+        nodes = np.frombuffer(ctypes.string_at(h.nodes, h.node_count * 32), dtype=BVH2_NODE_DTYPE).copy()
+    finally:
+        lib.nxb_free_host_bvh2(ctypes.byref(h))
+    return nodes, np.array([list(h.bounds.bmin), list(h.bounds.bmax)], dtype=np.float32)
+
+
+def save_bvh8(path, nodes: np.ndarray, prim_idx: np.ndarray, bounds) -> None:
+    """Writes host BVH8 nodes (BVH8_NODE_DTYPE), prim_idx and the root bounds
+    to a BVH file (nxb_write_bvh8)."""
+    nodes = np.ascontiguousarray(nodes, dtype=BVH8_NODE_DTYPE)
+    prim = np.ascontiguousarray(prim_idx, dtype=np.uint32)
+    h = CBVH8(nodes.ctypes.data, len(nodes), prim.ctypes.data, len(prim), _caabb(bounds))
+    check(load().nxb_write_bvh8(str(path).encode(), ctypes.byref(h)), "nxb_write_bvh8")
+
+
+def load_bvh8(path):
+    """(nodes as BVH8_NODE_DTYPE array, prim_idx uint32 array, bounds (2, 3))
+    read from a BVH file."""
+    lib = load()
+    h = CBVH8()
+    check(lib.nxb_read_bvh8(str(path).encode(), ctypes.byref(h)), "nxb_read_bvh8")
+    try:
+        nodes = np.frombuffer(ctypes.string_at(h.nodes, h.node_count * 80), dtype=BVH8_NODE_DTYPE).copy()
+        prim = np.frombuffer(ctypes.string_at(h.prim_idx, h.prim_count * 4), dtype=np.uint32).copy()
+    finally:
+        lib.nxb_free_host_bvh8(ctypes.byref(h))
+    return nodes, prim, np.array([list(h.bounds.bmin), list(h.bounds.bmax)], dtype=np.float32)
 
 
 def selftest_numerics() -> list[int]:

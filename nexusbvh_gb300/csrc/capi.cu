@@ -11,6 +11,7 @@
 //     stream-ordered (cudaMallocAsync from a pool that keeps its memory);
 //   * errors are returned as status codes: nothing calls cudaDeviceReset or
 //     exit (the reference's CUDA_CHECK does, NexusBVH/src/Cuda/CudaUtils.h:6-16).
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -272,6 +273,92 @@ nxb_status build_plain(const void* prims, nxb_prim_type type, uint32_t n, const 
     return e ? cuda_fail(e) : NXB_OK;
 }
 
+// ---- BVH files: a 64-byte header, the nodes, then (BVH8) prim_idx
+struct BvhFileHeader {
+    char magic[8];  // "NXBVH2\0\0" or "NXBVH8\0\0"
+    uint32_t version;
+    uint32_t node_count;
+    uint32_t prim_count;
+    uint32_t node_bytes;
+    nxb_aabb bounds;
+    uint8_t reserved[16];
+};
+static_assert(sizeof(BvhFileHeader) == 64, "BVH file header is 64 bytes");
+constexpr uint32_t kBvhFileVersion = 1;
+
+// Largest node count a BVH of prim_count primitives can have (BVH2: 2n-1;
+// BVH8: the reference's allocation, ceil((4n-1)/7), at least 1).
+uint64_t max_nodes(bool wide, uint32_t prim_count) {
+    if (prim_count == 0) return 0;
+    return wide ? std::max<uint64_t>(1, (4ull * prim_count - 1 + 6) / 7) : 2ull * prim_count - 1;
+}
+
+nxb_status write_bvh_file(const char* path, bool wide, const void* nodes, uint32_t node_count,
+                          const uint32_t* prim_idx, uint32_t prim_count, const nxb_aabb& bounds) {
+    if (!path || !nodes || node_count == 0 || prim_count == 0) return NXB_ERR_INVALID_ARGUMENT;
+    if (wide && !prim_idx) return NXB_ERR_INVALID_ARGUMENT;
+    if (node_count > max_nodes(wide, prim_count)) return NXB_ERR_INVALID_ARGUMENT;
+    BvhFileHeader h{};
+    std::memcpy(h.magic, wide ? "NXBVH8\0\0" : "NXBVH2\0\0", 8);
+    h.version = kBvhFileVersion;
+    h.node_count = node_count;
+    h.prim_count = prim_count;
+    h.node_bytes = wide ? sizeof(nxb_bvh8_node) : sizeof(nxb_bvh2_node);
+    h.bounds = bounds;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return NXB_ERR_IO;
+    bool ok = std::fwrite(&h, sizeof h, 1, f) == 1 &&
+              std::fwrite(nodes, h.node_bytes, node_count, f) == node_count &&
+              (!wide || std::fwrite(prim_idx, sizeof(uint32_t), prim_count, f) == prim_count);
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? NXB_OK : NXB_ERR_IO;
+}
+
+// Reads and checks a BVH file; on success *nodes and (BVH8) *prim_idx are
+// malloc'd and owned by the caller.
+nxb_status read_bvh_file(const char* path, bool wide, void** nodes, uint32_t* node_count, uint32_t** prim_idx,
+                         uint32_t* prim_count, nxb_aabb* bounds) {
+    if (!path) return NXB_ERR_INVALID_ARGUMENT;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return NXB_ERR_IO;
+    BvhFileHeader h{};
+    const size_t node_bytes = wide ? sizeof(nxb_bvh8_node) : sizeof(nxb_bvh2_node);
+    bool ok = std::fread(&h, sizeof h, 1, f) == 1 &&
+              std::memcmp(h.magic, wide ? "NXBVH8\0\0" : "NXBVH2\0\0", 8) == 0 && h.version == kBvhFileVersion &&
+              h.node_bytes == node_bytes && h.prim_count > 0 && h.node_count > 0 &&
+              h.node_count <= max_nodes(wide, h.prim_count);
+    long size = -1;
+    if (ok && std::fseek(f, 0, SEEK_END) == 0) size = std::ftell(f);
+    const uint64_t want = sizeof h + (uint64_t)h.node_count * node_bytes + (wide ? 4ull * h.prim_count : 0ull);
+    ok = ok && size >= 0 && (uint64_t)size == want && std::fseek(f, (long)sizeof h, SEEK_SET) == 0;
+    void* n = nullptr;
+    uint32_t* p = nullptr;
+    if (ok) {
+        n = std::malloc(node_bytes * h.node_count);
+        p = wide ? (uint32_t*)std::malloc(4ull * h.prim_count) : nullptr;
+        if (!n || (wide && !p)) {
+            std::free(n);
+            std::free(p);
+            std::fclose(f);
+            return NXB_ERR_OUT_OF_MEMORY;
+        }
+        ok = std::fread(n, node_bytes, h.node_count, f) == h.node_count &&
+             (!wide || std::fread(p, sizeof(uint32_t), h.prim_count, f) == h.prim_count);
+    }
+    std::fclose(f);
+    if (!ok) {
+        std::free(n);
+        std::free(p);
+        return NXB_ERR_IO;
+    }
+    *nodes = n;
+    *node_count = h.node_count;
+    if (wide) *prim_idx = p;
+    *prim_count = h.prim_count;
+    *bounds = h.bounds;
+    return NXB_OK;
+}
+
 }  // namespace
 
 nxb_status record_cuda_error(cudaError_t e) { return cuda_fail(e); }
@@ -312,6 +399,7 @@ const char* nxb_status_string(nxb_status s) {
         case NXB_ERR_DEVICE_TIMEOUT: return "NXB_ERR_DEVICE_TIMEOUT";
         case NXB_ERR_DEVICE_INVARIANT: return "NXB_ERR_DEVICE_INVARIANT";
         case NXB_ERR_ADMISSION: return "NXB_ERR_ADMISSION";
+        case NXB_ERR_IO: return "NXB_ERR_IO";
     }
     return "NXB_ERR_UNKNOWN";
 }
@@ -400,6 +488,39 @@ nxb_status nxb_free_device_bvh8(nxb_bvh8* d) {
     d->prim_idx = nullptr;
     if (e) return cuda_fail(e);
     return e2 ? cuda_fail(e2) : NXB_OK;
+}
+
+nxb_status nxb_write_bvh2(const char* path, const nxb_bvh2* h) {
+    if (!h) return NXB_ERR_INVALID_ARGUMENT;
+    return write_bvh_file(path, false, h->nodes, h->node_count, nullptr, h->prim_count, h->bounds);
+}
+
+nxb_status nxb_read_bvh2(const char* path, nxb_bvh2* h) {
+    if (!h) return NXB_ERR_INVALID_ARGUMENT;
+    nxb_bvh2 out{};
+    void* nodes = nullptr;
+    const nxb_status st = read_bvh_file(path, false, &nodes, &out.node_count, nullptr, &out.prim_count, &out.bounds);
+    if (st != NXB_OK) return st;
+    out.nodes = (nxb_bvh2_node*)nodes;
+    *h = out;
+    return NXB_OK;
+}
+
+nxb_status nxb_write_bvh8(const char* path, const nxb_bvh8* h) {
+    if (!h) return NXB_ERR_INVALID_ARGUMENT;
+    return write_bvh_file(path, true, h->nodes, h->node_count, h->prim_idx, h->prim_count, h->bounds);
+}
+
+nxb_status nxb_read_bvh8(const char* path, nxb_bvh8* h) {
+    if (!h) return NXB_ERR_INVALID_ARGUMENT;
+    nxb_bvh8 out{};
+    void* nodes = nullptr;
+    const nxb_status st =
+        read_bvh_file(path, true, &nodes, &out.node_count, &out.prim_idx, &out.prim_count, &out.bounds);
+    if (st != NXB_OK) return st;
+    out.nodes = (nxb_bvh8_node*)nodes;
+    *h = out;
+    return NXB_OK;
 }
 
 nxb_status nxb_query_build_sizes(uint32_t n, const nxb_build_config* config, nxb_build_sizes* out) {

@@ -260,3 +260,41 @@ def test_auction_assignment(gpu, orc, name, make, key_bits):
     out = nxb.Builder().build(S.dev(prims), nxb.BuildConfig(prioritize_speed=key_bits == 30, auction=True))
     b8p = S.host(out.nodes.reshape(-1)).view(nxb.BVH8_NODE_DTYPE)
     assert orc.compare_bvh8(b8p, S.host(out.prim_idx).view(np.uint32), b8_g, prim_g, n) == 0
+
+
+@pytest.mark.gpu
+def test_bvh8_file_round_trip_of_a_gpu_build(gpu, orc, tmp_path):
+    """A BVH8 built on the GPU, copied to the host through the C ABI
+    (nxb_bvh8_to_host), written to a file and read back is byte-identical and
+    still a valid tree over its primitives."""
+    import ctypes
+    import torch
+    prims = scenes.uniform_soup(20000, seed=21)
+    n = prims.shape[0]
+    cfg = nxb.BuildConfig(prioritize_speed=True).to_c()
+    d = torch.from_numpy(prims).cuda()
+    dev, host = nxb.CBVH8(), nxb.CBVH8()
+    nxb.check(gpu.nxb_build_bvh8(d.data_ptr(), nxb.NXB_PRIM_TRIANGLE, n, ctypes.byref(cfg), None, ctypes.byref(dev),
+                                 None), "nxb_build_bvh8")
+    try:
+        nxb.check(gpu.nxb_bvh8_to_host(ctypes.byref(dev), ctypes.byref(host)), "nxb_bvh8_to_host")
+        path = str(tmp_path / "gpu.nxb8").encode()
+        nxb.check(gpu.nxb_write_bvh8(path, ctypes.byref(host)), "nxb_write_bvh8")
+        back = nxb.CBVH8()
+        nxb.check(gpu.nxb_read_bvh8(path, ctypes.byref(back)), "nxb_read_bvh8")
+        try:
+            assert back.node_count == host.node_count and back.prim_count == host.prim_count == n
+            assert ctypes.string_at(back.nodes, 80 * back.node_count) == ctypes.string_at(host.nodes,
+                                                                                         80 * host.node_count)
+            assert ctypes.string_at(back.prim_idx, 4 * n) == ctypes.string_at(host.prim_idx, 4 * n)
+            assert list(back.bounds.bmin) == list(host.bounds.bmin)
+            nodes = np.frombuffer(ctypes.string_at(back.nodes, 80 * back.node_count), dtype=orc.NODE8).copy()
+            prim = np.frombuffer(ctypes.string_at(back.prim_idx, 4 * n), dtype=np.uint32).copy()
+            leaves, _ = orc.scene_bounds(prims)
+            errs, rep = orc.validate_bvh8(nodes, prim, n, leaves)
+            assert errs == 0, rep
+        finally:
+            gpu.nxb_free_host_bvh8(ctypes.byref(back))
+    finally:
+        gpu.nxb_free_host_bvh8(ctypes.byref(host))
+        gpu.nxb_free_device_bvh8(ctypes.byref(dev))
