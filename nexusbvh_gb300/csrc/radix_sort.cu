@@ -87,11 +87,14 @@ __global__ __launch_bounds__(kThreads, 4) void onesweep_kernel(const K* __restri
     const uint32_t mask = (1u << bits) - 1u;
     if (tid == 0) s_tile = atomicAdd(tile_ctr, 1u);
     for (int i = tid; i < kWarps * kRadixBins; i += kThreads) s_whist[i] = 0;
-    // global start of each digit: exclusive scan of this pass's histogram
-    const uint32_t digit_base = cta_exclusive_scan(tid <= mask ? hist[tid] : 0u, s_tmp);
+    __syncthreads();
     const uint32_t tile = s_tile;
     const uint32_t tile_base = tile * (uint32_t)TILE;
     if (tile_base >= n) return;  // only reachable when a launch claims more tiles than exist
+    // global start of each digit (exclusive scan of this pass's histogram):
+    // only tile 0 needs it, the others inherit it through the look-back
+    uint32_t digit_base = 0;
+    if (tile == 0) digit_base = cta_exclusive_scan(tid <= mask ? hist[tid] : 0u, s_tmp);
 
     // ---- load (warp-striped: warp w owns a contiguous run of 32*KPT keys)
     K key[KPT];
