@@ -152,19 +152,24 @@ def make_prims(name: str) -> np.ndarray:
     return scenes.by_name(name)
 
 
-def cpu_baseline(prims: np.ndarray, key_bits: int, radius: int, sample: int) -> dict:
-    """The CPU oracle (multithreaded restatement) on a bounded prefix sample."""
+def cpu_baseline(prims: np.ndarray, key_bits: int, radius: int, sample: int, seconds: float = 10.0) -> dict:
+    """The CPU oracle (multithreaded restatement) on a bounded prefix sample,
+    built repeatedly for at least `seconds` of CPU work."""
     import oracle
     m = min(sample, prims.shape[0])
     sub = np.ascontiguousarray(prims[:m])
+    builds, stage = 0, np.zeros(5)
     t = time.perf_counter()
-    r = oracle.build(sub, key_bits, radius)
+    while builds == 0 or time.perf_counter() - t < seconds:
+        r = oracle.build(sub, key_bits, radius)
+        assert r["err"] == 0
+        stage += np.array(r["stage_ms"])
+        builds += 1
     dt = time.perf_counter() - t
-    assert r["err"] == 0
-    return {"value": round(m / dt / 1e6, 3), "unit": "Mtris/s", "cores": oracle.threads(), "kind": "port",
-            "sample": f"first {m:,} triangles of the workload, one full CPU build (bounds, Morton, radix sort, "
-                      f"H-PLOC, BVH8) in {dt:.2f} s",
-            "stage_ms": [round(x, 1) for x in r["stage_ms"]]}
+    return {"value": round(m * builds / dt / 1e6, 3), "unit": "Mtris/s", "cores": oracle.threads(), "kind": "port",
+            "sample": f"first {m:,} triangles of the workload, {builds} full CPU builds (bounds, Morton, radix sort, "
+                      f"H-PLOC, BVH8) in {dt:.1f} s",
+            "stage_ms": [round(x / builds, 1) for x in stage]}
 
 
 def run_ours(args, world, rank, local):
@@ -261,6 +266,34 @@ def run_ours(args, world, rank, local):
         e2e_s = float(t.item())
     e2e_value = world * n * e2e_steps / e2e_s / 1e6
 
+    # the same calls with the copy of step k+1 (on its own stream, into the
+    # other of two input buffers) overlapping the build of step k
+    copy_stream = torch.cuda.Stream()
+    d_ins = [d_in, torch.empty_like(d_prims)]
+    copied = [torch.cuda.Event(), torch.cuda.Event()]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(copy_stream):
+        d_ins[0].copy_(h_prims, non_blocking=True)
+    copied[0].record(copy_stream)
+    for k in range(e2e_steps):
+        cur = k % 2
+        stream.wait_event(copied[cur])
+        if k + 1 < e2e_steps:  # the other buffer's build (step k-1) has returned: the call synchronises
+            with torch.cuda.stream(copy_stream):
+                d_ins[1 - cur].copy_(h_prims, non_blocking=True)
+            copied[1 - cur].record(copy_stream)
+        nxb.check(lib.nxb_build_bvh8(d_ins[cur].data_ptr(), nxb.NXB_PRIM_TRIANGLE, n, ctypes.byref(c), sptr,
+                                     ctypes.byref(out), None), "nxb_build_bvh8")
+        nxb.check(lib.nxb_free_device_bvh8(ctypes.byref(out)), "nxb_free_device_bvh8")
+    torch.cuda.synchronize()
+    e2e_ov_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_ov_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ov_s = float(t.item())
+    e2e_ov_value = world * n * e2e_steps / e2e_ov_s / 1e6
+
     if rank != 0:
         return
     pk = peaks()
@@ -303,6 +336,9 @@ def run_ours(args, world, rank, local):
             "stage_sum_ms": round(sum(stage_ms.values()), 4),
             "stage_roofline": per_stage,
             "bvh8_nodes": int(result.bvh8_node_count),
+            "e2e_overlapped_copy": {"value": round(e2e_ov_value, 2), "unit": "Mtris/s",
+                                    "how": "the e2e calls with step k+1's host->device copy on a second stream "
+                                           "overlapping step k's build (supplementary; e2e is the serial loop)"},
         },
         "roofline": {
             "kernel": dominant,
