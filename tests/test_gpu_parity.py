@@ -125,6 +125,23 @@ def test_small_sizes(gpu, orc, n):
     run_chain(scenes.uniform_soup(n, seed=n + 1), 63, orc)
 
 
+# Sizes on and around the tile edges of the tiled kernels: 256-primitive
+# bounds/Morton tiles, 3,072-key (64-bit) and 4,096-key (32-bit) sort tiles,
+# 256-leaf H-PLOC refill chunks.
+TILE_EDGES = [255, 256, 257, 3071, 3072, 3073, 4095, 4096, 6145, 8191, 8192, 8193, 12289]
+
+
+@pytest.mark.parametrize("n", TILE_EDGES)
+def test_tile_edges_with_runs_of_equal_keys(gpu, orc, n):
+    """Clustered data in which every third triangle repeats its predecessor,
+    so runs of equal Morton keys cross tile edges: the sort must stay stable
+    across tiles and H-PLOC must break the ties by position."""
+    t = scenes.clustered(n, seed=n, components=4)
+    t[2::3] = t[1::3][: t[2::3].shape[0]]
+    run_chain(t, 30, orc)
+    run_chain(t, 63, orc)
+
+
 def test_degenerate_inputs(gpu, orc):
     # every triangle identical: all keys equal, ties broken by index
     t = np.tile(np.array([[0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9]], np.float32), (3000, 1))
