@@ -18,7 +18,10 @@
 //     lane i, the first minimum of the union area (compared as uint32 bit
 //     patterns) over candidates i+1, i-1, i+2, i-2, ..., i+R, i-R.  Each
 //     pair's area is computed once and sent back to the partner with one
-//     shuffle (7 shuffles per radius step instead of 10);
+//     shuffle (7 shuffles per radius step instead of 10); at radius 8 a lane
+//     fetches only 4 neighbour boxes, at the offsets of a difference cover
+//     of the distances 1..8, and every pair is computed by one lane and
+//     shuffled to both of its lanes (36 shuffles per round instead of 56);
 //   * the merge and the order-preserving compaction follow
 //     MergeClustersCreateBVH2Node (:71-124); internal nodes are numbered
 //     from the tokens of the clusters they absorb instead of from a global
@@ -52,10 +55,60 @@ __device__ __forceinline__ uint64_t delta(const MeshKey* k, uint32_t a, uint32_t
     return (((uint64_t)ka << 32) | (a - s)) ^ (((uint64_t)kb << 32) | (b - s));
 }
 
-template <int R>
+// COVER selects the difference-cover search at radius 8 (single-mesh
+// builds, where it measured faster; the batched kernel keeps the plain one).
+template <int R, bool COVER>
 __device__ __forceinline__ uint32_t nearest_neighbour(uint32_t num, const Box& cb) {
     const uint32_t lane = lane_id();
     uint32_t best = kInvalid, best_idx = kInvalid;
+    if constexpr (R == 8 && COVER) {
+        // The marks {0, 1, 2, 5, 8} have every distance 1..8 as a difference
+        // (1 = 1-0, 2 = 2-0, 3 = 5-2, 4 = 5-1, 5 = 5-0, 6 = 8-2, 7 = 8-1,
+        // 8 = 8-0).  Each lane fetches the boxes of lanes +1, +2, +5 and +8
+        // (4 boxes instead of 8) and computes, for each distance d, the area
+        // of the pair (lane + a_d, lane + a_d + d), lanes taken modulo 32; a
+        // pair that wraps or reaches past the last cluster is invalid.  Every
+        // pair of the window is thereby computed by exactly one lane, and its
+        // area is shuffled to the two lanes it belongs to: 36 shuffles per
+        // round instead of 56.  The union is grown in the same operand order
+        // as below (upper box grown by the lower one), so every area has the
+        // same bits, and the candidates are compared in the same order.
+        auto pair = [&](const Box& lo_box, const Box& hi_box, uint32_t a, uint32_t d) -> uint32_t {
+            if (((lane + a) & 31u) + d >= num) return kInvalid;
+            Box u = hi_box;
+            grow(u, lo_box);
+            return __float_as_uint(half_area(u));
+        };
+        auto pick = [&](uint32_t f, uint32_t a, uint32_t d) {
+            const uint32_t fwd = a ? __shfl_sync(kFullMask, f, (lane - a) & 31u) : f;
+            const uint32_t back = __shfl_sync(kFullMask, f, (lane - d - a) & 31u);
+            if (fwd < best) {
+                best = fwd;
+                best_idx = lane + d;
+            }
+            if (back < best) {
+                best = back;
+                best_idx = lane - d;
+            }
+        };
+        const Box b1 = shfl_box(cb, (lane + 1) & 31u);
+        const Box b2 = shfl_box(cb, (lane + 2) & 31u);
+        pick(pair(cb, b1, 0, 1), 0, 1);
+        pick(pair(cb, b2, 0, 2), 0, 2);
+        {
+            const Box b5 = shfl_box(cb, (lane + 5) & 31u);
+            const uint32_t f3 = pair(b2, b5, 2, 3), f4 = pair(b1, b5, 1, 4), f5 = pair(cb, b5, 0, 5);
+            pick(f3, 2, 3);
+            pick(f4, 1, 4);
+            pick(f5, 0, 5);
+        }
+        const Box b8 = shfl_box(cb, (lane + 8) & 31u);
+        const uint32_t f6 = pair(b2, b8, 2, 6), f7 = pair(b1, b8, 1, 7), f8 = pair(cb, b8, 0, 8);
+        pick(f6, 2, 6);
+        pick(f7, 1, 7);
+        pick(f8, 0, 8);
+        return best_idx;
+    }
 #pragma unroll
     for (uint32_t r = 1; r <= (uint32_t)R; ++r) {
         Box nb = shfl_box(cb, (lane + r) & 31u);
@@ -192,7 +245,7 @@ __device__ __forceinline__ MergeCtx mesh_ctx(const MergeCtx& all, const Seg& seg
 // PlocMerge (BinaryBuilder.cu:200-273, the merge part) for the range of
 // lane `owner`; `start` is the first sorted position of its mesh and m
 // addresses that mesh's nodes.
-template <int R>
+template <int R, bool COVER>
 __device__ __forceinline__ void merge_windows(uint32_t owner, uint32_t left, uint32_t right, uint32_t split,
                                               bool final, uint32_t start, uint32_t* cluster, const MergeCtx& m) {
     const uint32_t lane = lane_id();
@@ -250,7 +303,7 @@ __device__ __forceinline__ void merge_windows(uint32_t owner, uint32_t left, uin
             num = 1;
             break;
         }
-        const uint32_t nn = nearest_neighbour<R>(num, cb);
+        const uint32_t nn = nearest_neighbour<R, COVER>(num, cb);
         num = merge_step(m, num, nn, cid, ctok, cb);
     }
     // StoreIndices (BinaryBuilder.cu:59-69)
@@ -267,9 +320,9 @@ __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t 
     if constexpr (Seg::kBatch) {
         uint32_t start;
         const MergeCtx m = mesh_ctx<Seg>(all, seg, me, owner, start);
-        merge_windows<R>(owner, left, right, split, final, start, cluster, m);
+        merge_windows<R, false>(owner, left, right, split, final, start, cluster, m);
     } else {
-        merge_windows<R>(owner, left, right, split, final, 0u, cluster, all);
+        merge_windows<R, true>(owner, left, right, split, final, 0u, cluster, all);
     }
 }
 
@@ -290,8 +343,17 @@ __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t 
 // touch the shared counter less; too large leaves warps without work.
 constexpr uint32_t kLeafChunk = 256;
 
+// Resident CTAs per SM, measured on GB300: a single-mesh build at radius 8
+// keeps the four neighbour boxes of its difference-cover search in
+// registers (56 registers, 9 CTAs; at 40 registers it spills and loses its
+// gain); the batched kernel and the other radii run at 40 registers.
+template <int R, typename Seg>
+constexpr int hploc_ctas_per_sm() {
+    return (R == 8 && !Seg::kBatch) ? 9 : 12;
+}
+
 template <typename K, int R, typename Seg>
-__global__ __launch_bounds__(kThreads, 12) void hploc_kernel(const K* __restrict__ keys, uint32_t* cluster,
+__global__ __launch_bounds__(kThreads, hploc_ctas_per_sm<R, Seg>()) void hploc_kernel(const K* __restrict__ keys, uint32_t* cluster,
                                                          uint32_t* parent, Node2* nodes, Seg seg, uint32_t begin,
                                                          uint32_t* tok, uint32_t* parent_of_last, uint32_t* leaf_ctr,
                                                          uint32_t* err, uint32_t end) {
