@@ -148,7 +148,9 @@ struct MortonArgs {
     int seed;
 };
 
-template <typename K, bool HIST>
+// PASSES > 0: the pass count of the plan, known at compile time (8 for
+// 63-bit keys, 4 for 30-bit), so the histogram loop unrolls.
+template <typename K, bool HIST, int PASSES = 0>
 __global__ __launch_bounds__(kThreads) void morton_kernel(const Node2* __restrict__ nodes, uint32_t n, Control* ctrl,
                                                           K* __restrict__ keys, MortonArgs a) {
     __shared__ float s_scene[6];
@@ -195,10 +197,24 @@ __global__ __launch_bounds__(kThreads) void morton_kernel(const Node2* __restric
             if (a.parent) a.parent[i] = kInvalid;
         }
         if (HIST) {
+            if constexpr (PASSES > 0) {
+#pragma unroll
+                for (int p = 0; p < PASSES; ++p) {
+                    const uint32_t d = (uint32_t)(key >> a.pd.shift[p]) & a.pd.mask[p];
+                    if (p < PASSES / 2) {
+                        // low digits: neighbouring keys rarely share them,
+                        // so the warp-uniform test seldom pays for itself
+                        if (valid) atomicAdd(&s_hist[p * kRadixBins + d], 1u);
+                    } else {
+                        hist_add(s_hist + p * kRadixBins, d, valid);
+                    }
+                }
+            } else {
 #pragma unroll 1
-            for (int p = 0; p < a.pd.passes; ++p) {
-                uint32_t d = (uint32_t)(key >> a.pd.shift[p]) & a.pd.mask[p];
-                hist_add(s_hist + p * kRadixBins, d, valid);
+                for (int p = 0; p < a.pd.passes; ++p) {
+                    uint32_t d = (uint32_t)(key >> a.pd.shift[p]) & a.pd.mask[p];
+                    hist_add(s_hist + p * kRadixBins, d, valid);
+                }
             }
         }
     }
@@ -499,12 +515,16 @@ cudaError_t launch_morton(const Node2* nodes, uint32_t n, Control* ctrl, int key
     a.seed = f.seed_counters ? 1 : 0;
     uint32_t grid = grid_for(n, 8);
     if (key_bits == 30) {
-        if (f.plan)
+        if (f.plan && a.pd.passes == 4)
+            morton_kernel<uint32_t, true, 4><<<grid, kThreads, 0, s>>>(nodes, n, ctrl, (uint32_t*)keys, a);
+        else if (f.plan)
             morton_kernel<uint32_t, true><<<grid, kThreads, 0, s>>>(nodes, n, ctrl, (uint32_t*)keys, a);
         else
             morton_kernel<uint32_t, false><<<grid, kThreads, 0, s>>>(nodes, n, ctrl, (uint32_t*)keys, a);
     } else {
-        if (f.plan)
+        if (f.plan && a.pd.passes == 8)
+            morton_kernel<uint64_t, true, 8><<<grid, kThreads, 0, s>>>(nodes, n, ctrl, (uint64_t*)keys, a);
+        else if (f.plan)
             morton_kernel<uint64_t, true><<<grid, kThreads, 0, s>>>(nodes, n, ctrl, (uint64_t*)keys, a);
         else
             morton_kernel<uint64_t, false><<<grid, kThreads, 0, s>>>(nodes, n, ctrl, (uint64_t*)keys, a);
