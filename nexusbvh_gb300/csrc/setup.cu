@@ -379,7 +379,7 @@ __global__ __launch_bounds__(T) void batch_bounds_kernel(const float* __restrict
 // kernel, and the same fill work (parent slots, look-back flags).  Tiles of
 // 256 elements: a tile inside one mesh reads the mesh's span and scene box
 // once, into shared memory.
-template <bool HIST, int T>
+template <bool HIST, int T, int PASSES = 0>
 __global__ __launch_bounds__(T) void batch_morton_kernel(const Node2* __restrict__ nodes, MeshBatch batch,
                                                                 uint32_t total, const uint32_t* scene_ord,
                                                                 uint64_t* __restrict__ keys, uint32_t* vals,
@@ -430,10 +430,22 @@ __global__ __launch_bounds__(T) void batch_morton_kernel(const Node2* __restrict
             vals[i] = local;
         }
         if (HIST) {
+            if constexpr (PASSES > 0) {
+#pragma unroll
+                for (int p = 0; p < PASSES; ++p) {
+                    const uint32_t d = (uint32_t)(key >> a.pd.shift[p]) & a.pd.mask[p];
+                    if (p < PASSES / 2) {
+                        if (valid) atomicAdd(&s_hist[p * kRadixBins + d], 1u);
+                    } else {
+                        hist_add(s_hist + p * kRadixBins, d, valid);
+                    }
+                }
+            } else {
 #pragma unroll 1
-            for (int p = 0; p < a.pd.passes; ++p) {
-                uint32_t d = (uint32_t)(key >> a.pd.shift[p]) & a.pd.mask[p];
-                hist_add(s_hist + p * kRadixBins, d, valid);
+                for (int p = 0; p < a.pd.passes; ++p) {
+                    uint32_t d = (uint32_t)(key >> a.pd.shift[p]) & a.pd.mask[p];
+                    hist_add(s_hist + p * kRadixBins, d, valid);
+                }
             }
         }
     }
@@ -592,15 +604,29 @@ cudaError_t launch_batch_morton(const Node2* nodes, const MeshBatch& batch, uint
     a.zero_vec4 = f.zero_words / 4;
     a.ones_ptr = reinterpret_cast<uint4*>(f.ones_ptr);
     a.ones_vec4 = f.ones_words / 4;
-    if (block == 128)
-        batch_morton_kernel<true, 128><<<batch_grid<128>(total), 128, 0, s>>>(nodes, batch, total, scene_ord, keys,
-                                                                              vals, hist, a);
-    else if (block == 512)
-        batch_morton_kernel<true, 512><<<batch_grid<512>(total), 512, 0, s>>>(nodes, batch, total, scene_ord, keys,
-                                                                              vals, hist, a);
-    else
-        batch_morton_kernel<true, 256><<<batch_grid<256>(total), 256, 0, s>>>(nodes, batch, total, scene_ord, keys,
-                                                                              vals, hist, a);
+    const bool five = a.pd.passes == 5;  // 8-bit digits over 40 bits: 1024 meshes
+    if (block == 128) {
+        if (five)
+            batch_morton_kernel<true, 128, 5><<<batch_grid<128>(total), 128, 0, s>>>(nodes, batch, total, scene_ord,
+                                                                                    keys, vals, hist, a);
+        else
+            batch_morton_kernel<true, 128><<<batch_grid<128>(total), 128, 0, s>>>(nodes, batch, total, scene_ord, keys,
+                                                                                  vals, hist, a);
+    } else if (block == 512) {
+        if (five)
+            batch_morton_kernel<true, 512, 5><<<batch_grid<512>(total), 512, 0, s>>>(nodes, batch, total, scene_ord,
+                                                                                    keys, vals, hist, a);
+        else
+            batch_morton_kernel<true, 512><<<batch_grid<512>(total), 512, 0, s>>>(nodes, batch, total, scene_ord, keys,
+                                                                                  vals, hist, a);
+    } else {
+        if (five)
+            batch_morton_kernel<true, 256, 5><<<batch_grid<256>(total), 256, 0, s>>>(nodes, batch, total, scene_ord,
+                                                                                    keys, vals, hist, a);
+        else
+            batch_morton_kernel<true, 256><<<batch_grid<256>(total), 256, 0, s>>>(nodes, batch, total, scene_ord, keys,
+                                                                                  vals, hist, a);
+    }
     return cudaGetLastError();
 }
 
