@@ -21,7 +21,9 @@
 //     shuffle (7 shuffles per radius step instead of 10); at radius 8 a lane
 //     fetches only 4 neighbour boxes, at the offsets of a difference cover
 //     of the distances 1..8, and every pair is computed by one lane and
-//     shuffled to both of its lanes (36 shuffles per round instead of 56);
+//     shuffled to both of its lanes (36 shuffles per round instead of 56;
+//     at radius 16, 8 fetches and 72 shuffles instead of 16 and 112; at
+//     radius 4, 3 fetches and 23 shuffles instead of 4 and 28);
 //   * the merge and the order-preserving compaction follow
 //     MergeClustersCreateBVH2Node (:71-124); internal nodes are numbered
 //     from the tokens of the clusters they absorb instead of from a global
@@ -55,13 +57,45 @@ __device__ __forceinline__ uint64_t delta(const MeshKey* k, uint32_t a, uint32_t
     return (((uint64_t)ka << 32) | (a - s)) ^ (((uint64_t)kb << 32) | (b - s));
 }
 
-// COVER selects the difference-cover search at radius 8 (single-mesh
-// builds, where it measured faster; the batched kernel keeps the plain one).
+// COVER selects the difference-cover search (single-mesh builds, where it
+// measured faster at every radius; the batched kernel keeps the plain one).
 template <int R, bool COVER>
 __device__ __forceinline__ uint32_t nearest_neighbour(uint32_t num, const Box& cb) {
     const uint32_t lane = lane_id();
     uint32_t best = kInvalid, best_idx = kInvalid;
-    if constexpr (R == 8 && COVER) {
+    if constexpr (R == 4 && COVER) {
+        // marks {0, 1, 2, 4}: 1 = 1-0, 2 = 2-0, 3 = 4-1, 4 = 4-0
+        auto pair = [&](const Box& lo_box, const Box& hi_box, uint32_t a, uint32_t d) -> uint32_t {
+            if (((lane + a) & 31u) + d >= num) return kInvalid;
+            Box u = hi_box;
+            grow(u, lo_box);
+            return __float_as_uint(half_area(u));
+        };
+        auto pick = [&](uint32_t f, uint32_t a, uint32_t d) {
+            const uint32_t fwd = a ? __shfl_sync(kFullMask, f, (lane - a) & 31u) : f;
+            const uint32_t back = __shfl_sync(kFullMask, f, (lane - d - a) & 31u);
+            if (fwd < best) {
+                best = fwd;
+                best_idx = lane + d;
+            }
+            if (back < best) {
+                best = back;
+                best_idx = lane - d;
+            }
+        };
+        const Box b1 = shfl_box(cb, (lane + 1) & 31u);
+        pick(pair(cb, b1, 0, 1), 0, 1);
+        {
+            const Box b2 = shfl_box(cb, (lane + 2) & 31u);
+            pick(pair(cb, b2, 0, 2), 0, 2);
+        }
+        const Box b4 = shfl_box(cb, (lane + 4) & 31u);
+        const uint32_t f3 = pair(b1, b4, 1, 3), f4 = pair(cb, b4, 0, 4);
+        pick(f3, 1, 3);
+        pick(f4, 0, 4);
+        return best_idx;
+    }
+    if constexpr ((R == 8 || R == 16) && COVER) {
         // The marks {0, 1, 2, 5, 8} have every distance 1..8 as a difference
         // (1 = 1-0, 2 = 2-0, 3 = 5-2, 4 = 5-1, 5 = 5-0, 6 = 8-2, 7 = 8-1,
         // 8 = 8-0).  Each lane fetches the boxes of lanes +1, +2, +5 and +8
@@ -102,11 +136,37 @@ __device__ __forceinline__ uint32_t nearest_neighbour(uint32_t num, const Box& c
             pick(f4, 1, 4);
             pick(f5, 0, 5);
         }
-        const Box b8 = shfl_box(cb, (lane + 8) & 31u);
-        const uint32_t f6 = pair(b2, b8, 2, 6), f7 = pair(b1, b8, 1, 7), f8 = pair(cb, b8, 0, 8);
-        pick(f6, 2, 6);
-        pick(f7, 1, 7);
-        pick(f8, 0, 8);
+        {
+            const Box b8 = shfl_box(cb, (lane + 8) & 31u);
+            const uint32_t f6 = pair(b2, b8, 2, 6), f7 = pair(b1, b8, 1, 7), f8 = pair(cb, b8, 0, 8);
+            pick(f6, 2, 6);
+            pick(f7, 1, 7);
+            pick(f8, 0, 8);
+        }
+        if constexpr (R == 16) {
+            // distances 9..16 are 8 + (1..8): the same low boxes 0, 1, 2
+            // against the boxes of lanes +9, +10, +13 and +16
+            {
+                const Box b9 = shfl_box(cb, (lane + 9) & 31u);
+                pick(pair(cb, b9, 0, 9), 0, 9);
+            }
+            {
+                const Box b10 = shfl_box(cb, (lane + 10) & 31u);
+                pick(pair(cb, b10, 0, 10), 0, 10);
+            }
+            {
+                const Box b13 = shfl_box(cb, (lane + 13) & 31u);
+                const uint32_t f11 = pair(b2, b13, 2, 11), f12 = pair(b1, b13, 1, 12), f13 = pair(cb, b13, 0, 13);
+                pick(f11, 2, 11);
+                pick(f12, 1, 12);
+                pick(f13, 0, 13);
+            }
+            const Box b16 = shfl_box(cb, (lane + 16) & 31u);
+            const uint32_t f14 = pair(b2, b16, 2, 14), f15 = pair(b1, b16, 1, 15), f16 = pair(cb, b16, 0, 16);
+            pick(f14, 2, 14);
+            pick(f15, 1, 15);
+            pick(f16, 0, 16);
+        }
         return best_idx;
     }
 #pragma unroll
@@ -343,13 +403,15 @@ __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t 
 // touch the shared counter less; too large leaves warps without work.
 constexpr uint32_t kLeafChunk = 256;
 
-// Resident CTAs per SM, measured on GB300: a single-mesh build at radius 8
-// keeps the four neighbour boxes of its difference-cover search in
-// registers (56 registers, 9 CTAs; at 40 registers it spills and loses its
-// gain); the batched kernel and the other radii run at 40 registers.
+// Resident CTAs per SM, measured on GB300: a single-mesh build keeps the
+// neighbour boxes of its difference-cover search in registers (radius 8:
+// 56 registers, 9 CTAs; radius 16: 64 registers, 8 CTAs; with fewer
+// registers they spill and lose the gain); the batched kernel and radius 4
+// (3 boxes) run at 40 registers.
 template <int R, typename Seg>
 constexpr int hploc_ctas_per_sm() {
-    return (R == 8 && !Seg::kBatch) ? 9 : 12;
+    if constexpr (Seg::kBatch) return 12;
+    return R == 8 ? 9 : (R == 16 ? 8 : 12);
 }
 
 template <typename K, int R, typename Seg>
