@@ -436,6 +436,9 @@ typedef struct nxb_server_stats {
     size_t bytes_in_use, peak_bytes_in_use;
 } nxb_server_stats;
 
+/* Creates a server on the current device.  Before returning it runs one tiny build through
+ * each pipeline it serves at the default radius (plain 30- and 63-bit, batched; triangles and
+ * boxes), so that the CUDA runtime has loaded those kernels before the first request arrives. */
 nxb_status nxb_server_create(const nxb_server_config* config, nxb_server** out_server);
 /* Waits for the builds in flight, then frees everything (unreleased results too). */
 nxb_status nxb_server_destroy(nxb_server* server);

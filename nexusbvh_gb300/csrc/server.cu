@@ -17,6 +17,7 @@
 //   * completion is signalled by a host function enqueued after the build,
 //     which only flips an atomic flag and wakes the worker; the worker then
 //     reads the per-build error word and counts from pinned memory.
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -399,6 +400,60 @@ void fill_result(const Request* r, nxb_server_result* out) {
     out->latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
 }
 
+// One tiny build through each pipeline a server runs at the default radius:
+// plain 30-bit and 63-bit, and batched, for triangles and boxes.  The CUDA
+// runtime loads a kernel on its first launch (lazy module loading); without
+// this, the first batched build of a server's life stalls the worker thread
+// for tens of milliseconds while every request behind it waits.
+nxb_status warm_up(cudaStream_t st) {
+    constexpr uint32_t kTris = 96, kMeshes = 2;
+    std::vector<float> h(9 * kTris);
+    for (uint32_t k = 0; k < kTris; ++k) {
+        const float x = (float)(k % 7), y = (float)(k / 7 % 5), z = (float)(k / 35);
+        const float v[9] = {x, y, z, x + 0.5f, y, z + 0.25f, x, y + 0.5f, z + 0.5f};
+        std::memcpy(&h[9 * k], v, sizeof v);
+    }
+    std::vector<float> hb(6 * kTris);  // the triangles' boxes
+    for (uint32_t k = 0; k < kTris; ++k)
+        for (int a = 0; a < 3; ++a) {
+            const float* t = &h[9 * k];
+            hb[6 * k + a] = std::min(t[a], std::min(t[3 + a], t[6 + a]));
+            hb[6 * k + 3 + a] = std::max(t[a], std::max(t[3 + a], t[6 + a]));
+        }
+    void* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(float) * (h.size() + hb.size()));
+    if (e) return record_cuda_error(e);
+    float* d_tri = static_cast<float*>(d);
+    float* d_box = d_tri + h.size();
+    e = cudaMemcpy(d_tri, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(d_box, hb.data(), sizeof(float) * hb.size(), cudaMemcpyHostToDevice);
+    nxb_status st_out = e ? record_cuda_error(e) : NXB_OK;
+    const uint32_t off[kMeshes + 1] = {0, kTris / 2, kTris};
+    for (int type = 0; type < 2 && st_out == NXB_OK; ++type) {
+        const nxb_prim_type pt = type ? NXB_PRIM_TRIANGLE : NXB_PRIM_AABB;
+        const void* prims = type ? (const void*)d_tri : (const void*)d_box;
+        for (uint32_t fast = 0; fast < 2 && st_out == NXB_OK; ++fast) {
+            nxb_build_config cfg{};
+            cfg.prioritize_speed = fast;
+            nxb_bvh8 out{};
+            st_out = nxb_build_bvh8(prims, pt, kTris, &cfg, st, &out, nullptr);
+            if (st_out == NXB_OK) nxb_free_device_bvh8(&out);
+        }
+        if (st_out == NXB_OK) {
+            nxb_build_config cfg{};
+            cfg.prioritize_speed = 1;
+            nxb_batch* b = nullptr;
+            st_out = nxb_batch_create(pt, off, kMeshes, &cfg, &b);
+            if (st_out == NXB_OK) {
+                st_out = nxb_batch_build(b, prims, st, nullptr);
+                nxb_batch_destroy(b);
+            }
+        }
+    }
+    cudaFree(d);
+    return st_out;
+}
+
 }  // namespace
 
 extern "C" {
@@ -448,6 +503,11 @@ nxb_status nxb_server_create(const nxb_server_config* config, nxb_server** out) 
         const nxb_status st = record_cuda_error(e);
         destroy_server(s);
         return st;
+    }
+    const nxb_status wst = warm_up(s->slots[0].stream);
+    if (wst != NXB_OK) {
+        destroy_server(s);
+        return wst;
     }
     s->worker = std::thread(worker_main, s);
     *out = s;
