@@ -389,7 +389,7 @@ __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t 
 // The climb with lane refill.  Each lane climbs from a leaf as in the
 // reference (FindParentId, exchange on the parent's hand-over slot, merge
 // and continue when second to arrive), but a lane that stops takes the next
-// unclaimed leaf from its warp's chunk (chunks of kLeafChunk leaves are
+// unclaimed leaf from its warp's chunk (chunks of `chunk` leaves are
 // claimed with one atomicAdd), instead of idling until every lane of its
 // warp has finished: the reference runs one thread per leaf, and a warp
 // stays resident for as long as any of its lanes still climbs (most stop
@@ -400,8 +400,16 @@ __device__ __noinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t 
 // Chunk size, measured on GB300 (12.58M clustered triangles, 6,080 resident
 // warps): 64 -> 2.91 ms, 256 -> 2.68 ms, 1024 -> 2.90 ms, 4096 -> 5.33 ms.
 // Larger chunks keep more of each subtree's climb inside one warp and
-// touch the shared counter less; too large leaves warps without work.
-constexpr uint32_t kLeafChunk = 256;
+// touch the shared counter less; too large leaves warps without work.  So
+// the chunk is about two per resident warp, rounded to a multiple of 32
+// between 32 and a cap (384 for one mesh, 256 for a batch: the best
+// measured caps).  65,536 triangles: 32 (H-PLOC 0.162 -> 0.125 ms against a
+// fixed 256); 4.19M: 384 (0.655 -> 0.614 ms); 12.58M: 384 (2.52 ms, as 256).
+uint32_t leaf_chunk(uint32_t leaves, uint32_t warps, bool batch) {
+    const uint32_t cap = batch ? 256u : 384u;
+    const uint32_t c = (leaves / (2u * std::max(warps, 1u)) + 16u) / 32u * 32u;
+    return std::max(32u, std::min(c, cap));
+}
 
 // Resident CTAs per SM, measured on GB300: a single-mesh build keeps the
 // neighbour boxes of its difference-cover search in registers (radius 8:
@@ -418,7 +426,7 @@ template <typename K, int R, typename Seg>
 __global__ __launch_bounds__(kThreads, hploc_ctas_per_sm<R, Seg>()) void hploc_kernel(const K* __restrict__ keys, uint32_t* cluster,
                                                          uint32_t* parent, Node2* nodes, Seg seg, uint32_t begin,
                                                          uint32_t* tok, uint32_t* parent_of_last, uint32_t* leaf_ctr,
-                                                         uint32_t* err, uint32_t end) {
+                                                         uint32_t* err, uint32_t end, uint32_t chunk) {
     const uint32_t lane = lane_id();
     const MergeCtx all{nodes, tok, parent_of_last, end, 2 * end - 1, err};
     uint32_t left = 0, right = 0, split = 0;
@@ -433,14 +441,14 @@ __global__ __launch_bounds__(kThreads, hploc_ctas_per_sm<R, Seg>()) void hploc_k
         while (need && !exhausted) {
             if (chunk_next == chunk_end) {
                 uint32_t b = 0;
-                if (lane == 0) b = begin + atomicAdd(leaf_ctr, kLeafChunk);
+                if (lane == 0) b = begin + atomicAdd(leaf_ctr, chunk);
                 b = __shfl_sync(kFullMask, b, 0);
                 if (b >= end) {
                     exhausted = true;
                     break;
                 }
                 chunk_next = b;
-                chunk_end = min(b + kLeafChunk, end);
+                chunk_end = min(b + chunk, end);
             }
             const uint32_t avail = chunk_end - chunk_next;
             const uint32_t rank = __popc(need & lanemask_lt());
@@ -502,8 +510,9 @@ cudaError_t launch_r(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* 
     if (per_sm < 1) per_sm = 1;
     const uint32_t want = (end - begin + kThreads - 1) / kThreads;
     const uint32_t grid = std::max(1u, std::min(want, (uint32_t)(device_info().sms * per_sm)));
+    const uint32_t chunk = leaf_chunk(end - begin, grid * (kThreads / 32), Seg::kBatch);
     hploc_kernel<K, R, Seg><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, seg, begin, tok, pol, leaf_ctr,
-                                                      err, end);
+                                                      err, end, chunk);
     return cudaGetLastError();
 }
 
