@@ -39,7 +39,7 @@ uint32_t mesh_bits_of(uint32_t meshes) { return meshes > 1 ? 32u - (uint32_t)__b
 
 // Segment offsets of an arena, in allocation order.
 struct Segments {
-    size_t off, off8, ctrl, scene, zero_end, parent, look, ctr8, mnodes, mleaves, ka, kb, va, vb, pairs, bvh2, bvh8,
+    size_t off, off8, ctrl, scene, zero_end, parent, look, ctr8, mnodes, mleaves, trng, ka, kb, va, vb, pairs, bvh2, bvh8,
         prim, res, total;
 };
 
@@ -62,6 +62,7 @@ Segments segments_of(const BatchArena& a) {
     g.ctr8 = seg(4 * kBvh8CtrWords * kMaxMeshGroups);
     g.mnodes = seg(4 * M);
     g.mleaves = seg(4 * M);
+    g.trng = seg(8 * ((n + 127) / 128));
     g.ka = seg(8 * n);
     g.kb = seg(8 * n);
     g.va = seg(4 * n);
@@ -117,6 +118,7 @@ void batch_bind(unsigned char* p, BatchArena* a) {
     a->ctr8 = reinterpret_cast<uint32_t*>(p + g.ctr8);
     a->mesh_nodes = reinterpret_cast<uint32_t*>(p + g.mnodes);
     a->mesh_leaves = reinterpret_cast<uint32_t*>(p + g.mleaves);
+    a->tile_rng = reinterpret_cast<uint2*>(p + g.trng);
     a->keys_a = reinterpret_cast<uint64_t*>(p + g.ka);
     a->keys_b = reinterpret_cast<uint64_t*>(p + g.kb);
     a->vals_a = reinterpret_cast<uint32_t*>(p + g.va);
@@ -158,14 +160,15 @@ nxb_status batch_enqueue(const BatchArena& a, const void* prims, nxb_prim_type t
     const SortPlan plan = make_sort_plan(2, 32 + a.mesh_bits, t.digit_bits);
     NXB_TRY(cudaMemsetAsync(a.zero_begin, 0, a.zero_bytes, s));
     if (a.total > 0) {
-        NXB_TRY(launch_batch_bounds(prims, type, mb, a.total, a.bvh2, a.scene_ord, t.block, s));
+        NXB_TRY(launch_batch_tile_ranges(mb, a.total, t.block, a.tile_rng, s));
+        NXB_TRY(launch_batch_bounds(prims, type, mb, a.total, a.bvh2, a.scene_ord, t.block, a.tile_rng, s));
         MortonFused f{};
         f.zero_ptr = a.lookback;
         f.zero_words = align_up(4 * a.lookback_words_per_pass * plan.passes) / 4;
         f.ones_ptr = a.parent;
         f.ones_words = a.ones_words;
         NXB_TRY(launch_batch_morton(a.bvh2, mb, a.total, a.scene_ord, a.keys_a, a.vals_a, plan, &a.ctrl->hist[0][0],
-                                    f, t.block, s));
+                                    f, t.block, a.tile_rng, s));
         for (int p = 0; p < plan.passes; ++p) {
             const bool even = (p % 2) == 0;
             NXB_TRY(launch_sort_pass(8, even ? a.keys_a : a.keys_b, even ? a.keys_b : a.keys_a,

@@ -112,13 +112,18 @@ cudaError_t launch_bvh8(const Node2* bvh2, uint32_t n, Node8* out, uint32_t cap,
 // common.cuh): one launch per stage for the whole batch.
 // scene_ord: 6 words per mesh, zero on entry.
 // block: CTA size of the two tile kernels (128, 256 or 512).
+// tile_rng: the first and last mesh of every `block`-primitive tile
+// (launch_batch_tile_ranges with the same block).
+cudaError_t launch_batch_tile_ranges(const MeshBatch& batch, uint32_t total, uint32_t block, uint2* tile_rng,
+                                     cudaStream_t s);
 cudaError_t launch_batch_bounds(const void* prims, int prim_type, const MeshBatch& batch, uint32_t total,
-                                Node2* nodes, uint32_t* scene_ord, uint32_t block, cudaStream_t s);
+                                Node2* nodes, uint32_t* scene_ord, uint32_t block, const uint2* tile_rng,
+                                cudaStream_t s);
 // keys: mesh << 32 | 30-bit code; vals: mesh-local primitive index; hist:
 // kMaxSortPasses x kRadixBins words, zero on entry.
 cudaError_t launch_batch_morton(const Node2* nodes, const MeshBatch& batch, uint32_t total, const uint32_t* scene_ord,
                                 uint64_t* keys, uint32_t* vals, const SortPlan& plan, uint32_t* hist,
-                                const MortonFused& fill, uint32_t block, cudaStream_t s);
+                                const MortonFused& fill, uint32_t block, const uint2* tile_rng, cudaStream_t s);
 // H-PLOC over the sorted positions [begin, end), which must cover whole
 // meshes; leaf_ctr: a zeroed word of its own.  parent_of_last: one word per
 // mesh holding INVALID on entry; ctas_per_sm caps the persistent grid (0: as
@@ -178,6 +183,7 @@ struct BatchArena {
     uint32_t* ctr8 = nullptr;
     uint32_t* mesh_nodes = nullptr;
     uint32_t* mesh_leaves = nullptr;
+    uint2* tile_rng = nullptr;  // mesh range of each bounds/Morton tile (up to total / 128 tiles)
     uint64_t* keys_a = nullptr;
     uint64_t* keys_b = nullptr;
     uint32_t* vals_a = nullptr;

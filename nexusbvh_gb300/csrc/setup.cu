@@ -263,10 +263,20 @@ __global__ __launch_bounds__(kThreads) void sort_histogram_kernel(const K* __res
 // ---------------------------------------------------------------- batches
 // The meshes of a tile's first and last element, found once per tile by
 // thread 0 (a mesh usually covers many tiles, so both are the same).
-__device__ __forceinline__ void tile_meshes(const MeshBatch& b, uint32_t first, uint32_t last, uint32_t* s_rng) {
+__device__ __forceinline__ uint2 tile_meshes(const MeshBatch& b, uint32_t first, uint32_t last) {
     const uint32_t lo = owner_of(b.off, 0, b.meshes - 1, first);
-    s_rng[0] = lo;
-    s_rng[1] = owner_of(b.off, lo, b.meshes - 1, last);
+    return make_uint2(lo, owner_of(b.off, lo, b.meshes - 1, last));
+}
+
+// The mesh range of every T-primitive tile, one thread per tile, so that the
+// tile kernels read it with one load instead of searching in one thread
+// while the others wait at a barrier.
+__global__ void batch_tile_ranges_kernel(MeshBatch batch, uint32_t total, uint32_t T, uint2* rng) {
+    const uint32_t tiles = (total + T - 1) / T;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < tiles; t += gridDim.x * blockDim.x) {
+        const uint32_t first = t * T;
+        rng[t] = tile_meshes(batch, first, min(first + T, total) - 1);
+    }
 }
 
 __device__ __forceinline__ void ord_max(uint32_t* o, const Box& b) {
@@ -300,9 +310,9 @@ __device__ __forceinline__ void warp_reduce_box(Box& b) {
 template <int FLOATS, int T>
 __global__ __launch_bounds__(T) void batch_bounds_kernel(const float* __restrict__ prims, MeshBatch batch,
                                                                 uint32_t total, Node2* __restrict__ nodes,
-                                                                uint32_t* scene_ord, bool aligned16) {
+                                                                uint32_t* scene_ord, bool aligned16,
+                                                                const uint2* __restrict__ tile_rng) {
     __shared__ __align__(16) float tile[T * FLOATS];
-    __shared__ uint32_t s_rng[2];
     __shared__ float s_red[T / 32][6];
     const uint32_t tiles = (total + T - 1) / T;
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
@@ -311,7 +321,7 @@ __global__ __launch_bounds__(T) void batch_bounds_kernel(const float* __restrict
         const uint32_t cnt = min((uint32_t)T, total - first);
         const float* src = prims + (size_t)first * FLOATS;
         __syncthreads();
-        if (threadIdx.x == 0) tile_meshes(batch, first, first + cnt - 1, s_rng);
+        const uint2 rng = __ldg(tile_rng + t);  // the tile's first and last mesh
         if (cnt == T && aligned16) {
             constexpr int V = T * FLOATS / 4;
             const float4* s4 = reinterpret_cast<const float4*>(src);
@@ -322,7 +332,7 @@ __global__ __launch_bounds__(T) void batch_bounds_kernel(const float* __restrict
             for (uint32_t v = threadIdx.x; v < cnt * FLOATS; v += T) tile[v] = __ldcs(src + v);
         }
         __syncthreads();
-        const uint32_t lo = s_rng[0], hi = s_rng[1];
+        const uint32_t lo = rng.x, hi = rng.y;
         const bool valid = threadIdx.x < cnt;
         const uint32_t g = first + min(threadIdx.x, cnt - 1);
         const MeshSpan me = batch.span(lo == hi ? lo : owner_of(batch.off, lo, hi, g));
@@ -383,41 +393,28 @@ template <bool HIST, int T, int PASSES = 0>
 __global__ __launch_bounds__(T) void batch_morton_kernel(const Node2* __restrict__ nodes, MeshBatch batch,
                                                                 uint32_t total, const uint32_t* scene_ord,
                                                                 uint64_t* __restrict__ keys, uint32_t* vals,
-                                                                uint32_t* hist, MortonArgs a) {
+                                                                uint32_t* hist, MortonArgs a,
+                                                                const uint2* __restrict__ tile_rng) {
     __shared__ uint32_t s_hist[HIST ? kMaxSortPasses * kRadixBins : 1];
-    __shared__ uint32_t s_rng[2];
-    __shared__ float s_scene[6];
     if (HIST)
         for (int i = threadIdx.x; i < a.pd.passes * kRadixBins; i += T) s_hist[i] = 0;
+    __syncthreads();
     const uint32_t tiles = (total + T - 1) / T;
     const uint32_t stride = gridDim.x * T;
     for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x) {
         const uint32_t first = t * T;
         const uint32_t cnt = min((uint32_t)T, total - first);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            tile_meshes(batch, first, first + cnt - 1, s_rng);
-            if (s_rng[0] == s_rng[1]) {
-                const uint32_t* o = scene_ord + 6ull * s_rng[0];
-                for (int k = 0; k < 6; ++k) s_scene[k] = ord2f(k < 3 ? ~o[k] : o[k]);
-            }
-        }
-        __syncthreads();
-        const uint32_t lo = s_rng[0], hi = s_rng[1];
+        const uint2 rng = __ldg(tile_rng + t);  // the tile's first and last mesh
+        const uint32_t lo = rng.x, hi = rng.y;
         const uint32_t i = first + threadIdx.x;
         const bool valid = threadIdx.x < cnt;
         uint64_t key = 0;
         if (valid) {
             const MeshSpan me = batch.span(lo == hi ? lo : owner_of(batch.off, lo, hi, i));
-            float3 smin, smax;
-            if (lo == hi) {
-                smin = make_float3(s_scene[0], s_scene[1], s_scene[2]);
-                smax = make_float3(s_scene[3], s_scene[4], s_scene[5]);
-            } else {
-                const uint32_t* o = scene_ord + 6ull * me.m;
-                smin = make_float3(ord2f(~__ldg(o + 0)), ord2f(~__ldg(o + 1)), ord2f(~__ldg(o + 2)));
-                smax = make_float3(ord2f(__ldg(o + 3)), ord2f(__ldg(o + 4)), ord2f(__ldg(o + 5)));
-            }
+            // the mesh's scene box (one L1 line that the whole tile reads)
+            const uint32_t* o = scene_ord + 6ull * me.m;
+            const float3 smin = make_float3(ord2f(~__ldg(o + 0)), ord2f(~__ldg(o + 1)), ord2f(~__ldg(o + 2)));
+            const float3 smax = make_float3(ord2f(__ldg(o + 3)), ord2f(__ldg(o + 4)), ord2f(__ldg(o + 5)));
             const uint32_t local = i - me.start;
             const float4* p = reinterpret_cast<const float4*>(nodes + 2ull * me.start + local);
             float4 lo4 = __ldcs(p);
@@ -574,30 +571,39 @@ uint32_t batch_grid(uint32_t total) {
 
 template <int T>
 void bounds_t(const void* prims, int prim_type, const MeshBatch& batch, uint32_t total, Node2* nodes,
-              uint32_t* scene_ord, bool aligned, cudaStream_t s) {
+              uint32_t* scene_ord, bool aligned, const uint2* tile_rng, cudaStream_t s) {
     if (prim_type == NXB_PRIM_TRIANGLE)
         batch_bounds_kernel<9, T><<<batch_grid<T>(total), T, 0, s>>>((const float*)prims, batch, total, nodes,
-                                                                     scene_ord, aligned);
+                                                                     scene_ord, aligned, tile_rng);
     else
         batch_bounds_kernel<6, T><<<batch_grid<T>(total), T, 0, s>>>((const float*)prims, batch, total, nodes,
-                                                                     scene_ord, aligned);
+                                                                     scene_ord, aligned, tile_rng);
+}
+
+cudaError_t launch_batch_tile_ranges(const MeshBatch& batch, uint32_t total, uint32_t block, uint2* tile_rng,
+                                     cudaStream_t s) {
+    const uint32_t tiles = (total + block - 1) / block;
+    const uint32_t grid = std::max(1u, std::min<uint32_t>((tiles + 255) / 256, (uint32_t)device_info().sms * 4));
+    batch_tile_ranges_kernel<<<grid, 256, 0, s>>>(batch, total, block, tile_rng);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_batch_bounds(const void* prims, int prim_type, const MeshBatch& batch, uint32_t total,
-                                Node2* nodes, uint32_t* scene_ord, uint32_t block, cudaStream_t s) {
+                                Node2* nodes, uint32_t* scene_ord, uint32_t block, const uint2* tile_rng,
+                                cudaStream_t s) {
     const bool aligned = (reinterpret_cast<uintptr_t>(prims) & 15u) == 0;
     if (block == 128)
-        bounds_t<128>(prims, prim_type, batch, total, nodes, scene_ord, aligned, s);
+        bounds_t<128>(prims, prim_type, batch, total, nodes, scene_ord, aligned, tile_rng, s);
     else if (block == 512)
-        bounds_t<512>(prims, prim_type, batch, total, nodes, scene_ord, aligned, s);
+        bounds_t<512>(prims, prim_type, batch, total, nodes, scene_ord, aligned, tile_rng, s);
     else
-        bounds_t<256>(prims, prim_type, batch, total, nodes, scene_ord, aligned, s);
+        bounds_t<256>(prims, prim_type, batch, total, nodes, scene_ord, aligned, tile_rng, s);
     return cudaGetLastError();
 }
 
 cudaError_t launch_batch_morton(const Node2* nodes, const MeshBatch& batch, uint32_t total, const uint32_t* scene_ord,
                                 uint64_t* keys, uint32_t* vals, const SortPlan& plan, uint32_t* hist,
-                                const MortonFused& f, uint32_t block, cudaStream_t s) {
+                                const MortonFused& f, uint32_t block, const uint2* tile_rng, cudaStream_t s) {
     MortonArgs a{};
     a.pd = to_digits(plan);
     a.zero_ptr = reinterpret_cast<uint4*>(f.zero_ptr);
@@ -608,24 +614,24 @@ cudaError_t launch_batch_morton(const Node2* nodes, const MeshBatch& batch, uint
     if (block == 128) {
         if (five)
             batch_morton_kernel<true, 128, 5><<<batch_grid<128>(total), 128, 0, s>>>(nodes, batch, total, scene_ord,
-                                                                                    keys, vals, hist, a);
+                                                                                    keys, vals, hist, a, tile_rng);
         else
             batch_morton_kernel<true, 128><<<batch_grid<128>(total), 128, 0, s>>>(nodes, batch, total, scene_ord, keys,
-                                                                                  vals, hist, a);
+                                                                                  vals, hist, a, tile_rng);
     } else if (block == 512) {
         if (five)
             batch_morton_kernel<true, 512, 5><<<batch_grid<512>(total), 512, 0, s>>>(nodes, batch, total, scene_ord,
-                                                                                    keys, vals, hist, a);
+                                                                                    keys, vals, hist, a, tile_rng);
         else
             batch_morton_kernel<true, 512><<<batch_grid<512>(total), 512, 0, s>>>(nodes, batch, total, scene_ord, keys,
-                                                                                  vals, hist, a);
+                                                                                  vals, hist, a, tile_rng);
     } else {
         if (five)
             batch_morton_kernel<true, 256, 5><<<batch_grid<256>(total), 256, 0, s>>>(nodes, batch, total, scene_ord,
-                                                                                    keys, vals, hist, a);
+                                                                                    keys, vals, hist, a, tile_rng);
         else
             batch_morton_kernel<true, 256><<<batch_grid<256>(total), 256, 0, s>>>(nodes, batch, total, scene_ord, keys,
-                                                                                  vals, hist, a);
+                                                                                  vals, hist, a, tile_rng);
     }
     return cudaGetLastError();
 }
