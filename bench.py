@@ -535,7 +535,9 @@ def run_batch(args, world, rank, local):
         "e2e": {"value": round(e2e_value, 2), "unit": "Mtris/s", "h2d_bytes_per_step": 36 * n,
                 "d2h_bytes_per_step": 52 * meshes + 4,
                 "call": "nxb_batch_build (graph replay + wait + per-mesh results) after a pinned host->device copy"},
-        "gpu_launches": (6 + passes) * args.steps,
+        # per build: tile ranges, bounds, Morton, the sort passes, BVH8 queue
+        # init, H-PLOC, BVH8, finalize (one mesh group)
+        "gpu_launches": (7 + passes) * args.steps,
         "clocks": clocks.summary(),
     }
     if not args.no_cpu_baseline:
