@@ -317,6 +317,50 @@ nxb_status nxb_eval_bvh8_cost(const nxb_bvh8_node* d_nodes, uint32_t node_count,
                               const nxb_aabb* d_root_bounds, float* d_cost,
                               struct CUstream_st* stream);
 
+/* Device-side validity checks: the checks of an exhaustive tree validator,
+ * run data-parallel on the GPU so that a full-size tree is checked without
+ * copying it to the host (the reference has no validator; the trees are the
+ * ones BuildBVH2Kernel / BuildBVH8Kernel write, BinaryBuilder.cu:200-273,
+ * WideConverter.cu:225-330).  Enqueued on `stream` with no host
+ * synchronisation and no allocation; d_report (device) is overwritten when
+ * the work runs.  Scratch: nxb_validate_bvh2/8_scratch_bytes().  "Reached"
+ * means the node's chain of parent references ends at the root.
+ *
+ * BVH2: prim_count leaves, 2*prim_count-1 nodes, root `root`.  d_report gets
+ * NXB_BVH2_CHECK_FIELDS words: [0] nodes reached (root included), [1] leaves
+ * among them, [2] extra copies of primitives held by several reached leaves,
+ * [3] primitives held by no reached leaf, [4] reached internal nodes whose
+ * box is not bit for bit the union of their children's, [5] children of
+ * reached nodes not contained in their parent's box, [6] reached nodes with a
+ * child or primitive index out of range, [7] maximum depth (root 0), [8]
+ * extra parent references (beyond one per node, all of them for the root),
+ * [9] errors = [2]+[3]+[4]+[5]+[6]+[8] + ([0] != 2n-1) + ([1] != n).
+ * A tree is valid when [9] is 0. */
+#define NXB_BVH2_CHECK_FIELDS 10
+size_t nxb_validate_bvh2_scratch_bytes(uint32_t prim_count);
+nxb_status nxb_validate_bvh2(const nxb_bvh2_node* d_nodes, uint32_t prim_count, uint32_t root,
+                             uint64_t* d_report, void* d_scratch, size_t scratch_bytes,
+                             struct CUstream_st* stream);
+/* BVH8: node_count nodes rooted at node 0, d_prim_idx[prim_count]; the
+ * primitives (d_prims, prim_type) give the exact leaf boxes.  d_report gets
+ * NXB_BVH8_CHECK_FIELDS words: [0] nodes reached, [1] leaf slots among them,
+ * [2] extra copies of primitives, [3] primitives in no leaf slot, [4] bad
+ * indices (inner child out of range, extra references of a node or any of
+ * the root, leaf slot or primitive index out of range), [5] / [6] decoded
+ * lower / upper child bounds p + 2^(e-127)*q (evaluated in double) that lie
+ * inside the exact box of the child's primitives, per axis, [7] slots used,
+ * [8] maximum depth, [9] meta errors (an inner bit on an empty slot, or a
+ * meta byte other than 0x20|(24+slot) for an inner child and 0x20|rank for a
+ * leaf), [10] errors = [2]+[3]+[4]+[9] + ([0] != node_count) +
+ * ([1] != prim_count).  Conservativeness ([5], [6]) is reported and not
+ * counted in [10]. */
+#define NXB_BVH8_CHECK_FIELDS 11
+size_t nxb_validate_bvh8_scratch_bytes(uint32_t node_count, uint32_t prim_count);
+nxb_status nxb_validate_bvh8(const nxb_bvh8_node* d_nodes, uint32_t node_count,
+                             const uint32_t* d_prim_idx, uint32_t prim_count, const void* d_prims,
+                             nxb_prim_type prim_type, uint64_t* d_report, void* d_scratch,
+                             size_t scratch_bytes, struct CUstream_st* stream);
+
 /* ------------------------------------------------------------ batched builds */
 /* No counterpart in the reference's API, which builds one mesh per call
  * (NXB::BuildBVH8, NexusBVH/include/NXB/BVHBuilder.h:18-31).  A batch builds

@@ -158,6 +158,10 @@ _SIG = {
     "nxb_stage_bvh8_ex": (ctypes.c_int, [_P, _U32, _P, _P, _P, _P, ctypes.c_size_t, _U32, _P, _P]),
     "nxb_eval_bvh2_cost": (ctypes.c_int, [_P, _U32, _P, _P, _P]),
     "nxb_eval_bvh8_cost": (ctypes.c_int, [_P, _U32, _P, _P, _P]),
+    "nxb_validate_bvh2_scratch_bytes": (ctypes.c_size_t, [_U32]),
+    "nxb_validate_bvh2": (ctypes.c_int, [_P, _U32, _U32, _P, _P, ctypes.c_size_t, _P]),
+    "nxb_validate_bvh8_scratch_bytes": (ctypes.c_size_t, [_U32, _U32]),
+    "nxb_validate_bvh8": (ctypes.c_int, [_P, _U32, _P, _U32, _P, ctypes.c_int, _P, _P, ctypes.c_size_t, _P]),
     "nxb_selftest_numerics": (ctypes.c_int, [_P, _U32]),
     "nxb_selftest_bounded_waits": (ctypes.c_int, [_P]),
     "nxb_batch_create": (ctypes.c_int, [ctypes.c_int, _P, _U32, _P, ctypes.POINTER(ctypes.c_void_p)]),
@@ -605,6 +609,51 @@ def load_bvh8(path):
     finally:
         lib.nxb_free_host_bvh8(ctypes.byref(h))
     return nodes, prim, np.array([list(h.bounds.bmin), list(h.bounds.bmax)], dtype=np.float32)
+
+
+BVH2_CHECK_FIELDS = ("reached", "leaves", "dup_prims", "missing_prims", "bad_union", "not_contained", "bad_index",
+                     "max_depth", "extra_parents", "errors")
+BVH8_CHECK_FIELDS = ("reached", "leaves", "dup_prims", "missing_prims", "bad_index", "lo_not_conservative",
+                     "hi_not_conservative", "slots_used", "max_depth", "meta_errors", "errors")
+
+
+def _run_check(fn, fields, scratch_bytes, args, device, stream):
+    import torch
+    if scratch_bytes == 0:
+        raise ValueError("sizes out of range for the validator")
+    s = stream if stream is not None else torch.cuda.current_stream(device)
+    with torch.cuda.stream(s):
+        scratch = torch.empty(scratch_bytes, dtype=torch.uint8, device=device)
+        report = torch.empty(len(fields), dtype=torch.int64, device=device)
+        check(fn(*args, report.data_ptr(), scratch.data_ptr(), scratch_bytes, int(s.cuda_stream)), fn.__name__)
+        s.synchronize()
+    rep = dict(zip(fields, (int(v) for v in report.cpu().numpy().view(np.uint64))))
+    return rep["errors"], rep
+
+
+def validate_bvh2(nodes, prim_count: int, root: int | None = None, stream=None):
+    """Checks a BVH2 on the device (nxb_validate_bvh2): ``nodes`` is a CUDA
+    tensor holding the 2n-1 nodes (32 bytes each), ``root`` defaults to 2n-2.
+    Returns (errors, report); the tree is valid when errors is 0."""
+    lib = load()
+    n = int(prim_count)
+    root = 2 * n - 2 if root is None else int(root)
+    return _run_check(lib.nxb_validate_bvh2, BVH2_CHECK_FIELDS, lib.nxb_validate_bvh2_scratch_bytes(n),
+                      (nodes.data_ptr(), n, root), nodes.device, stream)
+
+
+def validate_bvh8(nodes, node_count: int, prim_idx, prims, stream=None):
+    """Checks a BVH8 on the device (nxb_validate_bvh8): ``nodes`` (80-byte
+    nodes, root 0) and ``prim_idx`` are CUDA tensors, ``prims`` the CUDA
+    tensor the tree was built over ([n, 9] triangles or [n, 6] boxes, whose
+    boxes the quantised child bounds are checked against).  Returns (errors,
+    report); the tree is valid when errors is 0."""
+    lib = load()
+    n = int(prims.shape[0])
+    m = int(node_count)
+    return _run_check(lib.nxb_validate_bvh8, BVH8_CHECK_FIELDS, lib.nxb_validate_bvh8_scratch_bytes(m, n),
+                      (nodes.data_ptr(), m, prim_idx.data_ptr(), n, prims.data_ptr(), prim_type_of(prims)),
+                      nodes.device, stream)
 
 
 def selftest_numerics() -> list[int]:

@@ -19,7 +19,7 @@ CSRC = PKG / "csrc"
 BUILD = ROOT / "_build"
 LIB = PKG / "libnxb_gb300.so"
 
-CUDA_SOURCES = ["setup.cu", "radix_sort.cu", "hploc.cu", "wide.cu", "eval.cu", "capi.cu", "batch.cu", "server.cu"]
+CUDA_SOURCES = ["setup.cu", "radix_sort.cu", "hploc.cu", "wide.cu", "eval.cu", "capi.cu", "batch.cu", "server.cu", "validate.cu"]
 # --use_fast_math matches the reference's compile flags; the numerics the
 # tree depends on are pinned in the sources and checked by the self-test.
 NVCC_FLAGS = [

@@ -37,6 +37,8 @@ nxb_status cuda_fail(cudaError_t e) {
     } while (0)
 
 constexpr size_t kAlign = 256;
+// Largest primitive count the validators take (2n-1 nodes fit in uint32).
+constexpr uint32_t kMaxValidatePrims = 0x7FFFFFFFu;
 size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
 uint32_t key_bits_of(const nxb_build_config* c) { return c && c->prioritize_speed ? 30u : 63u; }
@@ -713,6 +715,37 @@ nxb_status nxb_eval_bvh8_cost(const nxb_bvh8_node* d_nodes, uint32_t count, cons
                               struct CUstream_st* stream) {
     if (!d_nodes || !d_root || !d_cost || count == 0) return NXB_ERR_INVALID_ARGUMENT;
     NXB_TRY(launch_bvh8_cost(reinterpret_cast<const Node8*>(d_nodes), count, d_root, d_cost, stream));
+    return NXB_OK;
+}
+
+size_t nxb_validate_bvh2_scratch_bytes(uint32_t n) {
+    if (n == 0 || n > kMaxValidatePrims) return 0;
+    return validate_bvh2_scratch(n);
+}
+
+nxb_status nxb_validate_bvh2(const nxb_bvh2_node* d_nodes, uint32_t n, uint32_t root, uint64_t* d_report,
+                             void* d_scratch, size_t scratch_bytes, struct CUstream_st* stream) {
+    if (!d_nodes || !d_report || !d_scratch || n == 0 || n > kMaxValidatePrims || root >= 2 * n - 1)
+        return NXB_ERR_INVALID_ARGUMENT;
+    if (scratch_bytes < validate_bvh2_scratch(n)) return NXB_ERR_INVALID_ARGUMENT;
+    NXB_TRY(launch_validate_bvh2(reinterpret_cast<const Node2*>(d_nodes), n, root, d_report, d_scratch, stream));
+    return NXB_OK;
+}
+
+size_t nxb_validate_bvh8_scratch_bytes(uint32_t node_count, uint32_t n) {
+    if (node_count == 0 || n == 0 || n > kMaxValidatePrims) return 0;
+    return validate_bvh8_scratch(node_count, n);
+}
+
+nxb_status nxb_validate_bvh8(const nxb_bvh8_node* d_nodes, uint32_t node_count, const uint32_t* d_prim_idx,
+                             uint32_t n, const void* d_prims, nxb_prim_type prim_type, uint64_t* d_report,
+                             void* d_scratch, size_t scratch_bytes, struct CUstream_st* stream) {
+    if (!d_nodes || !d_prim_idx || !d_prims || !d_report || !d_scratch || node_count == 0 || n == 0 ||
+        n > kMaxValidatePrims || (prim_type != NXB_PRIM_AABB && prim_type != NXB_PRIM_TRIANGLE))
+        return NXB_ERR_INVALID_ARGUMENT;
+    if (scratch_bytes < validate_bvh8_scratch(node_count, n)) return NXB_ERR_INVALID_ARGUMENT;
+    NXB_TRY(launch_validate_bvh8(reinterpret_cast<const Node8*>(d_nodes), node_count, d_prim_idx, n, d_prims,
+                                 (int)prim_type, d_report, d_scratch, stream));
     return NXB_OK;
 }
 

@@ -231,6 +231,13 @@ nxb_status batch_enqueue(const BatchArena& a, const void* prims, nxb_prim_type t
 // ---------------------------------------------------------------- eval
 cudaError_t launch_bvh2_cost(const Node2* nodes, uint32_t count, const nxb_aabb* root, float* cost, cudaStream_t s);
 cudaError_t launch_bvh8_cost(const Node8* nodes, uint32_t count, const nxb_aabb* root, float* cost, cudaStream_t s);
+// Device-side validity checks (validate.cu); scratch sizes in bytes.
+size_t validate_bvh2_scratch(uint32_t n);
+size_t validate_bvh8_scratch(uint32_t node_count, uint32_t n);
+cudaError_t launch_validate_bvh2(const Node2* nodes, uint32_t n, uint32_t root, uint64_t* report, void* scratch,
+                                 cudaStream_t s);
+cudaError_t launch_validate_bvh8(const Node8* nodes, uint32_t node_count, const uint32_t* prim_idx, uint32_t n,
+                                 const void* prims, int prim_type, uint64_t* report, void* scratch, cudaStream_t s);
 // Same, with the node count read on the device from *count_ptr (<= cap).
 cudaError_t launch_bvh8_cost_dev(const Node8* nodes, const uint32_t* count_ptr, uint32_t cap, const nxb_aabb* root,
                                  float* cost, cudaStream_t s);

@@ -68,6 +68,30 @@ def test_workspace_sizes(lib):
     assert lib.nxb_query_build_sizes(0, None, ctypes.byref(s)) == 1
 
 
+def test_validator_argument_checks_need_no_device(lib):
+    def seg(b):
+        return (b + 255) // 256 * 256
+    n = 1000
+    need2 = lib.nxb_validate_bvh2_scratch_bytes(n)
+    assert need2 == seg(8 * (2 * n - 1)) + seg(4 * (2 * n - 1)) + seg(4 * n)
+    assert lib.nxb_validate_bvh2_scratch_bytes(0) == 0
+    assert lib.nxb_validate_bvh2_scratch_bytes(1 << 31) == 0
+    m = 300
+    need8 = lib.nxb_validate_bvh8_scratch_bytes(m, n)
+    assert need8 == seg(8 * m) + 3 * seg(4 * m) + seg(24 * m) + seg(4 * n)
+    assert lib.nxb_validate_bvh8_scratch_bytes(0, n) == 0 and lib.nxb_validate_bvh8_scratch_bytes(m, 0) == 0
+    # every call below is rejected before anything is enqueued
+    assert lib.nxb_validate_bvh2(None, n, 0, 16, 16, need2, None) == 1
+    assert lib.nxb_validate_bvh2(16, n, 2 * n - 1, 16, 16, need2, None) == 1
+    assert lib.nxb_validate_bvh2(16, n, 0, 16, 16, need2 - 1, None) == 1
+    assert lib.nxb_validate_bvh2(16, 0, 0, 16, 16, need2, None) == 1
+    assert lib.nxb_validate_bvh2(16, n, 0, None, 16, need2, None) == 1
+    assert lib.nxb_validate_bvh8(16, m, 16, n, 16, 7, 16, 16, need8, None) == 1
+    assert lib.nxb_validate_bvh8(16, m, 16, n, None, 1, 16, 16, need8, None) == 1
+    assert lib.nxb_validate_bvh8(16, m, 16, n, 16, 1, 16, 16, need8 - 1, None) == 1
+    assert lib.nxb_validate_bvh8(16, 0, 16, n, 16, 1, 16, 16, need8, None) == 1
+
+
 def test_struct_layouts():
     assert ctypes.sizeof(nxb.CAABB) == 24
     assert ctypes.sizeof(nxb.CBVH2) == 40 and ctypes.sizeof(nxb.CBVH8) == 56

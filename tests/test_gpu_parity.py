@@ -91,6 +91,10 @@ def run_chain(prims, key_bits, orc, radius=8):
     assert orc.compare_bvh2(b2_g, 2 * n - 2, b2_o, root_o, n) == 0, "BVH2 differs from the oracle"
     errs, rep = orc.validate_bvh2(b2_g, n, 2 * n - 2)
     assert errs == 0, rep
+    # the device validator reads the tree in place and reports the same fields
+    g_errs, g_rep = nxb.validate_bvh2(d_b2, n)
+    assert g_errs == 0 and g_rep["extra_parents"] == 0, g_rep
+    assert list(g_rep.values())[:8] == list(rep.values()), (g_rep, rep)
 
     b8_g, prim_g, nc, lc = S.stage_bvh8(d_b2, n)
     b8_o, prim_o, err8 = orc.bvh8(b2_g, n, 2 * n - 2)
@@ -99,6 +103,10 @@ def run_chain(prims, key_bits, orc, radius=8):
     assert orc.compare_bvh8(b8_g, prim_g, b8_o, prim_o, n) == 0, "BVH8 differs from the oracle"
     errs8, rep8 = orc.validate_bvh8(b8_g, prim_g, n, leaves_g)
     assert errs8 == 0, rep8
+    g_errs8, g_rep8 = nxb.validate_bvh8(S.dev(b8_g.view(np.uint8)), nc, S.dev(prim_g.view(np.int32)),
+                                        S.dev(prims.astype(np.float32)))
+    assert g_errs8 == 0, g_rep8
+    assert list(g_rep8.values())[:10] == list(rep8.values()), (g_rep8, rep8)
 
     rb = S.root_box(b2_g, 2 * n - 2)
     c2g, c2o = S.cost_bvh2(d_b2, 2 * n - 1, rb), orc.bvh2_cost(b2_g, rb)
@@ -315,3 +323,76 @@ def test_bvh8_file_round_trip_of_a_gpu_build(gpu, orc, tmp_path):
     finally:
         gpu.nxb_free_host_bvh8(ctypes.byref(host))
         gpu.nxb_free_device_bvh8(ctypes.byref(dev))
+
+
+def test_device_validators_flag_planted_mistakes(gpu, orc):
+    """Each mistake is planted in a host copy of a correct oracle tree; the
+    device validators read the uploaded copy (every index they follow is
+    range-checked first) and flag what the oracle's validators flag."""
+    prims = scenes.uniform_soup(4096, seed=1)
+    n = prims.shape[0]
+    r = orc.build(prims, 30)
+    root = r["root"]
+    d_prims = S.dev(prims.astype(np.float32))
+
+    def both2(b2):
+        g = nxb.validate_bvh2(S.dev(b2.view(np.uint8)), n, root)
+        return g, orc.validate_bvh2(b2, n, root)
+
+    def both8(b8, prim):
+        g = nxb.validate_bvh8(S.dev(b8.view(np.uint8)), b8.shape[0], S.dev(prim.view(np.int32)), d_prims)
+        return g, orc.validate_bvh8(b8, prim, n, r["bvh2"][:n])
+
+    (ge, g), (oe, o) = both2(r["bvh2"])
+    assert ge == 0 and oe == 0 and list(g.values())[:8] == list(o.values())
+    (ge, g), (oe, o) = both8(r["bvh8"], r["prim_idx"])
+    assert ge == 0 and oe == 0 and list(g.values())[:10] == list(o.values())
+
+    inner = np.nonzero(r["bvh2"]["left"] != orc.INVALID)[0]
+    # a child that escapes its parent
+    b2 = r["bvh2"].copy()
+    b2[b2[inner[5]]["left"]]["bmax"][0] += 1.0
+    (ge, g), (oe, o) = both2(b2)
+    assert ge > 0 and g["not_contained"] >= 1 and list(g.values())[:8] == list(o.values())
+    # a duplicated primitive
+    b2 = r["bvh2"].copy()
+    leaf = np.nonzero(b2["left"] == orc.INVALID)[0]
+    b2[leaf[0]]["right"] = b2[leaf[1]]["right"]
+    (ge, g), (oe, o) = both2(b2)
+    assert g["dup_prims"] == 1 and g["missing_prims"] == 1 and list(g.values())[:8] == list(o.values())
+    # a child index past the last node: its subtrees are no longer reached
+    b2 = r["bvh2"].copy()
+    b2[inner[7]]["right"] = 2 * n + 5
+    (ge, g), (oe, o) = both2(b2)
+    assert ge > 0 and oe > 0 and g["bad_index"] == o["bad_index"] == 1 and g["reached"] == o["visited"]
+    # a reference back to the root (a cycle; only the device validator, which
+    # does not walk, is run on it)
+    b2 = r["bvh2"].copy()
+    b2[inner[9]]["left"] = root
+    ge, g = nxb.validate_bvh2(S.dev(b2.view(np.uint8)), n, root)
+    assert ge > 0 and g["extra_parents"] >= 1 and g["reached"] < 2 * n - 1
+
+    # a BVH8 child box shrunk below its exact box
+    b8 = r["bvh8"].copy()
+    b8[0]["qhi"][0][0] = 0
+    b8[0]["qlo"][0][0] = 255
+    (ge, g), (oe, o) = both8(b8, r["prim_idx"])
+    assert g["hi_not_conservative"] + g["lo_not_conservative"] >= 1
+    assert list(g.values())[:10] == list(o.values())
+    # two swapped leaf primitives
+    p = r["prim_idx"].copy()
+    p[[0, 1]] = p[[1, 0]]
+    (ge, g), (oe, o) = both8(r["bvh8"], p)
+    assert list(g.values())[:10] == list(o.values())
+    # a wrong meta byte
+    b8 = r["bvh8"].copy()
+    occupied = np.nonzero(b8[0]["meta"])[0][0]
+    b8[0]["meta"][occupied] ^= 0x40
+    (ge, g), (oe, o) = both8(b8, r["prim_idx"])
+    assert ge > 0 and g["meta_errors"] >= 1 and oe > 0
+    # children renumbered onto the root: extra references and lost subtrees
+    b8 = r["bvh8"].copy()
+    k = int(np.nonzero(b8["imask"][1:])[0][0]) + 1
+    b8[k]["child_base"] = 0
+    (ge, g), (oe, o) = both8(b8, r["prim_idx"])
+    assert ge > 0 and oe > 0 and g["bad_index"] >= 1
