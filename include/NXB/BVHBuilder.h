@@ -42,7 +42,7 @@ inline nxb_build_config to_c(const BuildConfig& c) {
     nxb_build_config r{};
     r.prioritize_speed = c.prioritizeSpeed ? 1u : 0u;
     r.search_radius = c.searchRadius;
-    r.flags = c.useAuction ? NXB_BUILD_AUCTION : 0u;
+    r.flags = (c.useAuction ? NXB_BUILD_AUCTION : 0u) | (c.validate ? NXB_BUILD_VALIDATE : 0u);
     return r;
 }
 inline void from_c(const nxb_build_metrics& m, BVHBuildMetrics* out) {

@@ -16,6 +16,9 @@ struct BuildConfig {
     // BVH8 child slots by the auction algorithm (the reference's compile-time
     // USE_AUCTION) instead of the greedy assignment
     bool useAuction = false;
+    // check the trees on the device before returning (BuildBVH2 / BuildBVH8
+    // fail as on any other error when a tree is invalid)
+    bool validate = false;
 };
 
 }  // namespace NXB

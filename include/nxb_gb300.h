@@ -58,7 +58,8 @@ typedef enum nxb_status {
     NXB_ERR_CUDA = 4,             /* a CUDA runtime call failed (see nxb_last_cuda_error) */
     NXB_ERR_WORKSPACE_TOO_SMALL = 5,
     NXB_ERR_DEVICE_TIMEOUT = 6,   /* a bounded device-side wait gave up (error word set) */
-    NXB_ERR_DEVICE_INVARIANT = 7, /* a kernel found an impossible state (error word set) */
+    NXB_ERR_DEVICE_INVARIANT = 7, /* a kernel found an impossible state (error word set), or
+                                     NXB_BUILD_VALIDATE found an invalid tree */
     NXB_ERR_ADMISSION = 8,        /* server: the request does not fit the memory budget */
     NXB_ERR_IO = 9                /* a BVH file could not be opened, read or written, or is not
                                      a BVH file of this format */
@@ -146,6 +147,13 @@ typedef struct nxb_build_config {
  * NexusBVH/src/Cuda/WideConverter.cu:5,50-102,337-358; off in the reference's
  * build).  Same tree and boxes, different child order inside BVH8 nodes. */
 #define NXB_BUILD_AUCTION 0x1u
+/* Plain calls (nxb_build_bvh2 / nxb_build_bvh8) only: after the build, check
+ * the trees on the device (nxb_validate_bvh2, and nxb_validate_bvh8 for a
+ * BVH8 build, whose intermediate BVH2 is checked too) and return
+ * NXB_ERR_DEVICE_INVARIANT, with no tree, when one is invalid.  The other
+ * entry points answer NXB_ERR_UNSUPPORTED; their callers run the
+ * validators themselves. */
+#define NXB_BUILD_VALIDATE 0x2u
 
 /* -------------------------------------------- reference-shaped entry points */
 /* Builds a BVH2 from n device primitives (nxb_triangle or nxb_aabb).  The

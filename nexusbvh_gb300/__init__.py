@@ -123,6 +123,7 @@ assert ctypes.sizeof(CBVH2) == 40 and ctypes.sizeof(CBVH8) == 56 and ctypes.size
 assert ctypes.sizeof(CBatchMesh) == 52
 NXB_TUNE_RADIUS = 0x1
 NXB_BUILD_AUCTION = 0x1
+NXB_BUILD_VALIDATE = 0x2
 NXB_SERVER_RESERVE = 0x1
 
 _P = ctypes.c_void_p
@@ -223,10 +224,11 @@ class BuildConfig:
     prioritize_speed: bool = False
     search_radius: int = 8
     auction: bool = False
+    validate: bool = False  # plain builds: check the trees on the device before returning
 
     def to_c(self) -> CConfig:
-        return CConfig(1 if self.prioritize_speed else 0, int(self.search_radius),
-                       NXB_BUILD_AUCTION if self.auction else 0, 0)
+        flags = (NXB_BUILD_AUCTION if self.auction else 0) | (NXB_BUILD_VALIDATE if self.validate else 0)
+        return CConfig(1 if self.prioritize_speed else 0, int(self.search_radius), flags, 0)
 
     @property
     def key_bits(self) -> int:

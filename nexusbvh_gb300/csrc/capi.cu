@@ -87,11 +87,41 @@ Layout make_layout(uint32_t n, uint32_t key_bits) {
 
 size_t bvh8_capacity(uint32_t n) { return ((size_t)4 * n - 1 + 6) / 7; }
 
-nxb_status check_config(const nxb_build_config* c) {
+// allowed: the NXB_BUILD_* flags the calling entry point takes.
+nxb_status check_config(const nxb_build_config* c, uint32_t allowed = NXB_BUILD_AUCTION) {
     if (!c) return NXB_OK;
     uint32_t r = c->search_radius;
     if (r != 0 && r != 4 && r != 8 && r != 16) return NXB_ERR_UNSUPPORTED;
-    if (c->flags & ~NXB_BUILD_AUCTION) return NXB_ERR_UNSUPPORTED;
+    if (c->flags & ~allowed) return NXB_ERR_UNSUPPORTED;
+    return NXB_OK;
+}
+
+bool validate_of(const nxb_build_config* c) { return c && (c->flags & NXB_BUILD_VALIDATE); }
+
+// NXB_BUILD_VALIDATE: checks the BVH2 (root 2n-2) and, when bvh8 is given,
+// the BVH8 of a finished build on stream s; NXB_ERR_DEVICE_INVARIANT when
+// either is invalid.
+nxb_status validate_built(const void* prims, nxb_prim_type type, uint32_t n, const Node2* bvh2, const Node8* bvh8,
+                          const uint32_t* prim_idx, uint32_t bvh8_nodes, cudaStream_t s) {
+    size_t bytes = validate_bvh2_scratch(n);
+    if (bvh8) bytes = std::max(bytes, validate_bvh8_scratch(bvh8_nodes, n));
+    void* scratch = nullptr;
+    uint64_t* rep = nullptr;
+    uint64_t h2[NXB_BVH2_CHECK_FIELDS] = {}, h8[NXB_BVH8_CHECK_FIELDS] = {};
+    cudaError_t e = cudaMallocAsync(&scratch, bytes, s);
+    if (!e) e = cudaMallocAsync((void**)&rep, sizeof(h2) + sizeof(h8), s);
+    // one scratch for both checks: they run one after the other on s
+    if (!e) e = launch_validate_bvh2(bvh2, n, 2 * n - 2, rep, scratch, s);
+    if (!e && bvh8)
+        e = launch_validate_bvh8(bvh8, bvh8_nodes, prim_idx, n, prims, (int)type, rep + NXB_BVH2_CHECK_FIELDS, scratch,
+                                 s);
+    if (!e) e = cudaMemcpyAsync(h2, rep, sizeof(h2), cudaMemcpyDeviceToHost, s);
+    if (!e && bvh8) e = cudaMemcpyAsync(h8, rep + NXB_BVH2_CHECK_FIELDS, sizeof(h8), cudaMemcpyDeviceToHost, s);
+    if (!e) e = cudaStreamSynchronize(s);
+    if (scratch) cudaFreeAsync(scratch, s);
+    if (rep) cudaFreeAsync(rep, s);
+    if (e) return cuda_fail(e);
+    if (h2[NXB_BVH2_CHECK_FIELDS - 1] || h8[NXB_BVH8_CHECK_FIELDS - 1]) return NXB_ERR_DEVICE_INVARIANT;
     return NXB_OK;
 }
 
@@ -189,7 +219,7 @@ nxb_status build_plain(const void* prims, nxb_prim_type type, uint32_t n, const 
                        cudaStream_t s, bool wide, nxb_bvh2* out2, nxb_bvh8* out8, nxb_build_metrics* metrics) {
     nxb_status st = check_prims(prims, type, n);
     if (st != NXB_OK) return st;
-    if ((st = check_config(cfg)) != NXB_OK) return st;
+    if ((st = check_config(cfg, NXB_BUILD_AUCTION | NXB_BUILD_VALIDATE)) != NXB_OK) return st;
     configure_pool();
     const Layout L = make_layout(n, key_bits_of(cfg));
     unsigned char* ws = nullptr;
@@ -229,6 +259,8 @@ nxb_status build_plain(const void* prims, nxb_prim_type type, uint32_t n, const 
             if (!e) e = cudaStreamSynchronize(s);
             if (e) status = cuda_fail(e);
             if (status == NXB_OK) status = status_from_error_word(res.error_word);
+            if (status == NXB_OK && validate_of(cfg))
+                status = validate_built(prims, type, n, bvh2, wide ? bvh8 : nullptr, prim_idx, res.bvh8_node_count, s);
             if (status == NXB_OK && metrics) {
                 float t[5] = {0, 0, 0, 0, 0};
                 for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&t[i], evs.ev[i], evs.ev[i + 1]);

@@ -66,6 +66,10 @@ def test_workspace_sizes(lib):
         assert s.workspace_bytes >= n * (2 * kb + 8 + 4 + 8)
         assert s.workspace_bytes < n * (2 * kb + 8 + 4 + 8 + 8)
     assert lib.nxb_query_build_sizes(0, None, ctypes.byref(s)) == 1
+    # NXB_BUILD_VALIDATE belongs to the plain calls only
+    v = nxb.BuildConfig(validate=True).to_c()
+    assert v.flags == nxb.NXB_BUILD_VALIDATE
+    assert lib.nxb_query_build_sizes(1000, ctypes.byref(v), ctypes.byref(s)) == 2
 
 
 def test_validator_argument_checks_need_no_device(lib):

@@ -193,6 +193,15 @@ def test_pipeline_entry_points_agree(gpu, orc):
     assert orc.compare_bvh2(S.nodes2(p2.nodes.view(-1)), 2 * n - 2, chain["b2"], 2 * n - 2, n) == 0
     assert np.allclose(np.array(p2.bounds[0]), chain["b2"][2 * n - 2]["bmin"])
 
+    # NXB_BUILD_VALIDATE: the same trees, checked on the device before the call returns
+    m2 = nxb.BVHBuildMetrics()
+    v8 = nxb.build_bvh8(S.dev(prims), nxb.BuildConfig(validate=True), m2)
+    b8v = S.host(v8.nodes.reshape(-1)).view(nxb.BVH8_NODE_DTYPE)
+    assert orc.compare_bvh8(b8v, S.host(v8.prim_idx).view(np.uint32), chain["b8"], chain["prim"], n) == 0
+    assert abs(m2.bvh8_cost - chain["costs"][1]) <= 1e-3 * chain["costs"][1]
+    v2 = nxb.build_bvh2(S.dev(scenes.to_boxes(prims)), nxb.BuildConfig(prioritize_speed=True, validate=True))
+    assert v2.node_count == 2 * n - 1
+
 
 def test_numerics_selftest(gpu, orc):
     rep = nxb.selftest_numerics()
