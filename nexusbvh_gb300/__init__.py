@@ -619,6 +619,13 @@ BVH8_CHECK_FIELDS = ("reached", "leaves", "dup_prims", "missing_prims", "bad_ind
                      "hi_not_conservative", "slots_used", "max_depth", "meta_errors", "errors")
 
 
+def _device_bytes(t, what: str) -> int:
+    """Bytes a CUDA tensor holds; raises unless it is contiguous on a CUDA device."""
+    if not t.is_cuda or not t.is_contiguous():
+        raise ValueError(f"{what} must be a contiguous CUDA tensor")
+    return t.numel() * t.element_size()
+
+
 def _run_check(fn, fields, scratch_bytes, args, device, stream):
     import torch
     if scratch_bytes == 0:
@@ -640,6 +647,8 @@ def validate_bvh2(nodes, prim_count: int, root: int | None = None, stream=None):
     lib = load()
     n = int(prim_count)
     root = 2 * n - 2 if root is None else int(root)
+    if _device_bytes(nodes, "nodes") < (2 * n - 1) * 32:
+        raise ValueError("nodes holds fewer than 2n-1 BVH2 nodes")
     return _run_check(lib.nxb_validate_bvh2, BVH2_CHECK_FIELDS, lib.nxb_validate_bvh2_scratch_bytes(n),
                       (nodes.data_ptr(), n, root), nodes.device, stream)
 
@@ -650,9 +659,17 @@ def validate_bvh8(nodes, node_count: int, prim_idx, prims, stream=None):
     tensor the tree was built over ([n, 9] triangles or [n, 6] boxes, whose
     boxes the quantised child bounds are checked against).  Returns (errors,
     report); the tree is valid when errors is 0."""
+    import torch
     lib = load()
     n = int(prims.shape[0])
     m = int(node_count)
+    if _device_bytes(nodes, "nodes") < m * 80:
+        raise ValueError("nodes holds fewer than node_count BVH8 nodes")
+    if _device_bytes(prim_idx, "prim_idx") < n * 4:
+        raise ValueError("prim_idx holds fewer than n entries")
+    if prims.dtype != torch.float32:
+        raise ValueError("prims must be float32")
+    _device_bytes(prims, "prims")
     return _run_check(lib.nxb_validate_bvh8, BVH8_CHECK_FIELDS, lib.nxb_validate_bvh8_scratch_bytes(m, n),
                       (nodes.data_ptr(), m, prim_idx.data_ptr(), n, prims.data_ptr(), prim_type_of(prims)),
                       nodes.device, stream)

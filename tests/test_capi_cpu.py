@@ -175,3 +175,12 @@ def test_server_argument_checks_need_no_device(lib):
     assert lib.nxb_server_release(None, 1) == 1
     assert lib.nxb_server_destroy(None) == 1
     assert ctypes.sizeof(nxb.CServerResult) == 80 and ctypes.sizeof(nxb.CServerStats) == 64
+
+
+def test_validator_wrappers_check_tensors():
+    torch = pytest.importorskip("torch")
+    cpu = torch.zeros(64, dtype=torch.uint8)
+    with pytest.raises(ValueError):
+        nxb.validate_bvh2(cpu, 1)
+    with pytest.raises(ValueError):
+        nxb.validate_bvh8(cpu, 1, torch.zeros(1, dtype=torch.int32), torch.zeros((1, 9), dtype=torch.float32))
