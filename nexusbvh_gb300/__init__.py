@@ -474,6 +474,23 @@ class Batch:
             lib.nxb_free_host_bvh8(ctypes.byref(h))
         return nodes, prim
 
+    def validate_mesh(self, mesh: int, prims, meshes=None):
+        """Checks one mesh's BVH2 and BVH8 on the device, in place in the
+        batch's arrays (their indices are mesh-local, so each mesh is a
+        standalone tree); ``prims`` is the CUDA tensor the batch was built
+        from.  Returns ((errors, report) of the BVH2, (errors, report) of the
+        BVH8)."""
+        a = self.arrays()
+        info = (meshes or self.wait(results=True))[mesh]
+        n = int(info.prim_count)
+        if n == 0:
+            raise ValueError("an empty mesh has no tree")
+        b2 = _borrow(a.bvh2_nodes + info.bvh2_offset * 32, info.bvh2_node_count * 32)
+        b8 = _borrow(a.bvh8_nodes + info.bvh8_offset * 80, info.bvh8_node_count * 80)
+        pi = _borrow(a.prim_idx + info.prim_offset * 4, n * 4)
+        pm = prims[info.prim_offset:info.prim_offset + n]
+        return validate_bvh2(b2, n), validate_bvh8(b8, int(info.bvh8_node_count), pi, pm)
+
     def mesh_bvh2_host(self, mesh: int, meshes=None):
         """BVH2 nodes (BVH2_NODE_DTYPE, mesh-local child indices) of one mesh after a build."""
         import torch

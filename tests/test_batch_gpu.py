@@ -67,9 +67,13 @@ def test_batch_matches_oracle(gpu, orc):
     counts = [3000, 1, 0, 5000, 257]
     prims = make_batch(counts, seed=8)
     batch = nxb.Batch(counts)
-    meshes = batch.build(S.dev(prims))
+    d_prims = S.dev(prims)
+    meshes = batch.build(d_prims)
     off = np.concatenate([[0], np.cumsum(counts)])
     for m, n in enumerate(counts):
+        if n >= 1:  # every tree checked on the device in place, with the oracle's report
+            (e2, g2), (e8, g8) = batch.validate_mesh(m, d_prims, meshes)
+            assert e2 == 0 and e8 == 0 and g2["leaves"] == n and g8["leaves"] == n, (g2, g8)
         if n < 2:
             continue
         pm = prims[off[m]:off[m + 1]]
@@ -91,6 +95,7 @@ def test_batch_matches_oracle(gpu, orc):
         assert orc.compare_bvh8(b8, prim, b8_o, prim_o, n) == 0
         errs8, rep8 = orc.validate_bvh8(b8, prim, n, leaves)
         assert errs8 == 0, rep8
+        assert list(g2.values())[:8] == list(rep.values()) and list(g8.values())[:10] == list(rep8.values())
 
 
 @pytest.mark.parametrize("groups", [2, 4, 8])
