@@ -391,6 +391,10 @@ typedef struct nxb_batch_mesh {        /* per-mesh result, 52 B */
     uint32_t bvh8_node_count, bvh8_leaf_count;
 } nxb_batch_mesh;
 
+/* Indices are mesh-local, so each mesh's trees are standalone: nxb_validate_bvh2
+ * on bvh2_nodes + bvh2_offset (prim_count leaves, root 2n-2) and nxb_validate_bvh8
+ * on bvh8_nodes + bvh8_offset, prim_idx + prim_offset and the mesh's primitives
+ * check one mesh in place. */
 typedef struct nxb_batch_arrays {      /* device views owned by the batch */
     const nxb_bvh2_node* bvh2_nodes;   /* child indices are mesh-local */
     const nxb_bvh8_node* bvh8_nodes;   /* child_base / prim_base are mesh-local */
