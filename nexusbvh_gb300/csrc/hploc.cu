@@ -93,9 +93,7 @@ __device__ __forceinline__ uint32_t nearest_neighbour(uint32_t num, const Box& c
         const uint32_t f3 = pair(b1, b4, 1, 3), f4 = pair(cb, b4, 0, 4);
         pick(f3, 1, 3);
         pick(f4, 0, 4);
-        return best_idx;
-    }
-    if constexpr ((R == 8 || R == 16) && COVER) {
+    } else if constexpr ((R == 8 || R == 16) && COVER) {
         // The marks {0, 1, 2, 5, 8} have every distance 1..8 as a difference
         // (1 = 1-0, 2 = 2-0, 3 = 5-2, 4 = 5-1, 5 = 5-0, 6 = 8-2, 7 = 8-1,
         // 8 = 8-0).  Each lane fetches the boxes of lanes +1, +2, +5 and +8
@@ -167,24 +165,24 @@ __device__ __forceinline__ uint32_t nearest_neighbour(uint32_t num, const Box& c
             pick(f15, 1, 15);
             pick(f16, 0, 16);
         }
-        return best_idx;
-    }
+    } else {
 #pragma unroll
-    for (uint32_t r = 1; r <= (uint32_t)R; ++r) {
-        Box nb = shfl_box(cb, (lane + r) & 31u);
-        uint32_t a = kInvalid;
-        if (lane + r < num) {
-            grow(nb, cb);
-            a = __float_as_uint(half_area(nb));
-        }
-        const uint32_t back = __shfl_sync(kFullMask, a, (lane - r) & 31u);
-        if (a < best) {
-            best = a;
-            best_idx = lane + r;
-        }
-        if (back < best) {
-            best = back;
-            best_idx = lane - r;
+        for (uint32_t r = 1; r <= (uint32_t)R; ++r) {
+            Box nb = shfl_box(cb, (lane + r) & 31u);
+            uint32_t a = kInvalid;
+            if (lane + r < num) {
+                grow(nb, cb);
+                a = __float_as_uint(half_area(nb));
+            }
+            const uint32_t back = __shfl_sync(kFullMask, a, (lane - r) & 31u);
+            if (a < best) {
+                best = a;
+                best_idx = lane + r;
+            }
+            if (back < best) {
+                best = back;
+                best_idx = lane - r;
+            }
         }
     }
     return best_idx;
