@@ -7,7 +7,6 @@ imports this package.
 from __future__ import annotations
 
 import ctypes
-from pathlib import Path
 
 import numpy as np
 

@@ -2,7 +2,6 @@
 torch-allocated device buffers and return numpy arrays."""
 from __future__ import annotations
 
-import ctypes
 
 import numpy as np
 
