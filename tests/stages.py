@@ -2,7 +2,6 @@
 torch-allocated device buffers and return numpy arrays."""
 from __future__ import annotations
 
-
 import numpy as np
 
 import nexusbvh_gb300 as nxb
