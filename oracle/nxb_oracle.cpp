@@ -949,6 +949,10 @@ uint64_t orc_validate_bvh2(const void* nodes_v, uint32_t n, uint32_t root, uint6
             rep[6]++;
             continue;
         }
+        if (rep[0] == total) {  // more visits than nodes: a shared subtree or a cycle; stop the walk
+            rep[0]++;
+            break;
+        }
         rep[0]++;
         rep[7] = std::max<uint64_t>(rep[7], d);
         const Node2& nd = nodes[i];

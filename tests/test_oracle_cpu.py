@@ -163,6 +163,11 @@ def test_validators_catch_planted_mistakes(orc):
     b2[leaf[0]]["right"] = b2[leaf[1]]["right"]
     errs, rep = orc.validate_bvh2(b2, n, root)
     assert rep["dup_prims"] == 1 and rep["missing_prims"] == 1
+    # a cycle back to the root: the walk stops and reports errors
+    b2 = r["bvh2"].copy()
+    b2[inner]["left"] = root
+    errs, rep = orc.validate_bvh2(b2, n, root)
+    assert errs > 0 and rep["visited"] == 2 * n
     # a BVH8 child box shrunk below its exact box
     b8 = r["bvh8"].copy()
     b8[0]["qhi"][0][0] = 0
