@@ -184,3 +184,17 @@ def test_validator_wrappers_check_tensors():
         nxb.validate_bvh2(cpu, 1)
     with pytest.raises(ValueError):
         nxb.validate_bvh8(cpu, 1, torch.zeros(1, dtype=torch.int32), torch.zeros((1, 9), dtype=torch.float32))
+
+
+def test_every_cuda_source_is_built():
+    from nexusbvh_gb300 import _build
+    on_disk = sorted(p.name for p in (Path(nxb.__file__).parent / "csrc").glob("*.cu"))
+    assert sorted(_build.CUDA_SOURCES) == on_disk
+
+
+def test_check_report_lengths_match_the_header():
+    hdr = (Path(nxb.__file__).parent.parent / "include" / "nxb_gb300.h").read_text()
+    n2 = int(re.search(r"#define NXB_BVH2_CHECK_FIELDS (\d+)", hdr).group(1))
+    n8 = int(re.search(r"#define NXB_BVH8_CHECK_FIELDS (\d+)", hdr).group(1))
+    assert n2 == len(nxb.BVH2_CHECK_FIELDS) and n8 == len(nxb.BVH8_CHECK_FIELDS)
+    assert nxb.BVH2_CHECK_FIELDS[-1] == nxb.BVH8_CHECK_FIELDS[-1] == "errors"
