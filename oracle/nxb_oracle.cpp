@@ -1103,7 +1103,7 @@ uint64_t orc_compare_bvh2(const void* a_v, uint32_t a_root, const void* b_v, uin
         auto [ia, ib] = stack.back();
         stack.pop_back();
         ++pos;
-        if (ia >= total || ib >= total) return pos;
+        if (ia >= total || ib >= total || pos > total) return pos;  // pos > total: a cycle
         const Node2& x = a[ia];
         const Node2& y = b[ib];
         if (!same_box(x.b, y.b)) return pos;
@@ -1133,7 +1133,7 @@ uint64_t orc_compare_bvh8(const void* a_v, uint32_t a_count, const uint32_t* a_p
         auto [ia, ib] = stack.back();
         stack.pop_back();
         ++pos;
-        if (ia >= a_count || ib >= b_count) return pos;
+        if (ia >= a_count || ib >= b_count || pos > a_count) return pos;  // pos > a_count: a cycle
         const Node8& x = a[ia];
         const Node8& y = b[ib];
         if (std::memcmp(x.p, y.p, 12) || std::memcmp(x.e, y.e, 3) || x.imask != y.imask ||
@@ -1170,10 +1170,11 @@ static bool unordered_hashes(const Node8* nodes, uint32_t count, const uint32_t*
     node_h.assign(count, 0);
     child_h.assign(8ull * count, 0);
     std::vector<std::pair<uint32_t, bool>> stack = {{0, false}};
+    uint64_t pops = 0;
     while (!stack.empty()) {
         auto [i, expanded] = stack.back();
         stack.pop_back();
-        if (i >= count) return false;
+        if (i >= count || ++pops > 2ull * count) return false;  // each node is popped twice; more: a cycle
         const Node8& x = nodes[i];
         if (!expanded) {
             stack.push_back({i, true});
@@ -1227,7 +1228,7 @@ uint64_t orc_compare_bvh8_unordered(const void* a_v, uint32_t a_count, const uin
     while (!stack.empty()) {
         auto [ia, ib] = stack.back();
         stack.pop_back();
-        ++visited;
+        if (++visited > a_count) return 3;  // a cycle
         bool same = true;
         for (uint32_t s = 0; s < 8; ++s) same &= ca[8ull * ia + s] == cb[8ull * ib + s];
         if (!same) ++*reordered;
@@ -1262,11 +1263,11 @@ uint64_t orc_digest_bvh2(const void* nodes_v, uint32_t root, uint32_t n) {
     const Node2* nodes = (const Node2*)nodes_v;
     uint64_t h = 1469598103934665603ull;
     std::vector<uint32_t> stack = {root};
-    uint32_t total = 2 * n - 1;
+    uint32_t total = 2 * n - 1, visits = 0;
     while (!stack.empty()) {
         uint32_t i = stack.back();
         stack.pop_back();
-        if (i >= total) return 0;
+        if (i >= total || ++visits > total) return 0;
         const Node2& nd = nodes[i];
         fnv(h, &nd.b, sizeof(Box));
         uint32_t tag = nd.left == kInvalid ? nd.right : kInvalid;
@@ -1282,10 +1283,11 @@ uint64_t orc_digest_bvh8(const void* nodes_v, uint32_t count, const uint32_t* pr
     const Node8* nodes = (const Node8*)nodes_v;
     uint64_t h = 1469598103934665603ull;
     std::vector<uint32_t> stack = {0};
+    uint32_t visits = 0;
     while (!stack.empty()) {
         uint32_t i = stack.back();
         stack.pop_back();
-        if (i >= count) return 0;
+        if (i >= count || ++visits > count) return 0;
         const Node8& x = nodes[i];
         fnv(h, x.p, 12);
         fnv(h, x.e, 3);

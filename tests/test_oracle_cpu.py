@@ -163,11 +163,19 @@ def test_validators_catch_planted_mistakes(orc):
     b2[leaf[0]]["right"] = b2[leaf[1]]["right"]
     errs, rep = orc.validate_bvh2(b2, n, root)
     assert rep["dup_prims"] == 1 and rep["missing_prims"] == 1
-    # a cycle back to the root: the walk stops and reports errors
+    # a cycle back to the root: every walk stops (validate, compare, digest)
     b2 = r["bvh2"].copy()
     b2[inner]["left"] = root
     errs, rep = orc.validate_bvh2(b2, n, root)
     assert errs > 0 and rep["visited"] == 2 * n
+    assert orc.compare_bvh2(b2, root, b2, root, n) != 0
+    assert orc.digest_bvh2(b2, root, n) == 0
+    b8 = r["bvh8"].copy()
+    k = int(np.nonzero(b8["imask"][1:])[0][0]) + 1
+    b8[k]["child_base"] = 0
+    assert orc.compare_bvh8(b8, r["prim_idx"], b8, r["prim_idx"], n) != 0
+    assert orc.compare_bvh8_unordered(b8, r["prim_idx"], b8, r["prim_idx"], n)[0] != 0
+    assert orc.digest_bvh8(b8, r["prim_idx"], n) == 0
     # a BVH8 child box shrunk below its exact box
     b8 = r["bvh8"].copy()
     b8[0]["qhi"][0][0] = 0
