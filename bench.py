@@ -156,6 +156,7 @@ def cpu_baseline(prims: np.ndarray, key_bits: int, radius: int, sample: int, sec
     """The CPU oracle (multithreaded restatement) on a bounded prefix sample,
     built repeatedly for at least `seconds` of CPU work."""
     import oracle
+    oracle.set_level_collapse(True)  # every stage on all host threads
     m = min(sample, prims.shape[0])
     sub = np.ascontiguousarray(prims[:m])
     builds, stage = 0, np.zeros(5)
@@ -542,6 +543,7 @@ def run_batch(args, world, rank, local):
     }
     if not args.no_cpu_baseline:
         import oracle
+        oracle.set_level_collapse(True)
         t = time.perf_counter()
         done = 0
         m = 0
@@ -721,6 +723,7 @@ def run_reference(args, world, rank, local):
                           "call"}), flush=True)
         return
     import oracle
+    oracle.set_level_collapse(True)  # every stage on all host threads
 
     key_bits = args.key_bits
     if args.workload in BATCH_WORKLOADS:

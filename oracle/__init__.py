@@ -30,6 +30,7 @@ def load() -> ctypes.CDLL:
         U = ctypes.c_uint32
         sig = {
             "orc_set_threads": (None, [ctypes.c_int]),
+            "orc_set_level_collapse": (None, [ctypes.c_int]),
             "orc_get_threads": (ctypes.c_int, []),
             "orc_set_area_form": (None, [ctypes.c_int]),
             "orc_get_area_form": (ctypes.c_int, []),
@@ -140,16 +141,23 @@ def bvh8_capacity(n: int) -> int:
     return (4 * n - 1 + 6) // 7
 
 
-def bvh8(bvh2_nodes: np.ndarray, n: int, root: int, auction: bool = False):
+def set_level_collapse(on: bool) -> None:
+    """build(): BVH8 stage by the level-parallel collapse (the timed CPU
+    baseline) instead of the work-slot-order one (the default)."""
+    load().orc_set_level_collapse(1 if on else 0)
+
+
+def bvh8(bvh2_nodes: np.ndarray, n: int, root: int, auction: bool = False, levels: bool = False):
     """-> (nodes NODE8[count], prim_idx uint32[n], error bits); auction selects
-    the USE_AUCTION slot assignment (WideConverter.cu:50-102)."""
+    the USE_AUCTION slot assignment (WideConverter.cu:50-102); levels the
+    level-parallel collapse (same tree, breadth-first numbering)."""
     cap = bvh8_capacity(n)
     out = np.zeros(cap, dtype=NODE8)
     prim = np.zeros(n, dtype=np.uint32)
     nc = ctypes.c_uint32(0)
     lc = ctypes.c_uint32(0)
     err = load().orc_bvh8_ex(_p(np.ascontiguousarray(bvh2_nodes)), n, root, _p(out), cap, _p(prim),
-                             ctypes.byref(nc), ctypes.byref(lc), 1 if auction else 0)
+                             ctypes.byref(nc), ctypes.byref(lc), (1 if auction else 0) | (2 if levels else 0))
     return out[: nc.value].copy(), prim, err
 
 

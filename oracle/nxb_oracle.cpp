@@ -69,6 +69,9 @@ static_assert(sizeof(Node8) == 80, "BVH8 node is 80 bytes");
 
 // ------------------------------------------------------------- settings
 int g_threads = 0;    // 0 = hardware concurrency
+// orc_build's BVH8 stage: 0 = bvh8() (work-slot order), 1 = bvh8_levels()
+// (level-parallel; set where the build is timed as the CPU baseline)
+int g_level_collapse = 0;
 int g_area_form = 2;  // see area()
 int g_u8_mode = 0;    // 0: (uint8)(uint32 truncating convert); 1: saturate to [0,255]
 int g_min_zero = 0;   // 0: min(+0,-0) = -0 and max = +0 whatever the order
@@ -782,6 +785,107 @@ int bvh8(const Node2* nodes, uint32_t n, uint32_t root, Node8* out, uint32_t cap
     return err;
 }
 
+// One BVH8 node of bvh8_levels before it is numbered: its children (BVH2
+// indices), slot assignment and inner / leaf slot masks, exactly as one work
+// item of bvh8() computes them.
+struct CollapsedNode {
+    uint32_t child[8];
+    uint32_t asg, inner, leaf;
+};
+
+void collapse_node(const Node2* nodes, uint32_t b2, bool use_auction, CollapsedNode& c) {
+    const Node2& nd = nodes[b2];
+    uint32_t inner = 0, count = 0;
+    uint32_t lr[2] = {nd.left, nd.right};
+    int msb = 0;
+    while (true) {
+        float a0 = area(nodes[lr[0]].b), a1 = area(nodes[lr[1]].b);
+        uint32_t first = a0 < a1 ? 0 : 1;
+        for (uint32_t i = 0; i < 2; ++i) {
+            uint32_t idx = i == 0 ? (uint32_t)msb : count;
+            if (nodes[lr[first]].left != kInvalid) inner |= 1u << idx;
+            c.child[idx] = lr[first];
+            count++;
+            first = !first;
+        }
+        msb = inner ? 31 - __builtin_clz(inner) : -1;
+        if (msb < 0 || count == 8) break;
+        inner &= ~(1u << msb);
+        count--;
+        uint32_t ni = c.child[msb];
+        lr[0] = nodes[ni].left;
+        lr[1] = nodes[ni].right;
+    }
+    float pc[3];
+    for (int a = 0; a < 3; ++a) pc[a] = fadd(nd.b.mn[a], nd.b.mx[a]);
+    uint32_t asg = 0;
+    if (!use_auction || !auction(nd.b, c.child, count, nodes, &asg)) asg = greedy(pc, c.child, count, nodes);
+    c.asg = asg;
+    c.inner = c.leaf = 0;
+    for (uint32_t i = 0; i < 8; ++i) {
+        if (nib(asg, i) == 0xF) continue;
+        uint32_t bit = (inner >> nib(asg, i)) & 1u;
+        c.inner |= bit << i;
+        c.leaf |= (bit ^ 1u) << i;
+    }
+}
+
+// The same collapse level by level, for the timed CPU baseline: the nodes of
+// one BVH8 level are collapsed in parallel, numbered by a prefix sum over the
+// level, and written in parallel.  Nodes and primitive slots are numbered
+// breadth-first instead of in work-slot order, so the tree equals bvh8()'s
+// up to that numbering (canonically identical).
+int bvh8_levels(const Node2* nodes, uint32_t n, uint32_t root, Node8* out, uint32_t cap, uint32_t* prim_idx,
+                uint32_t* node_count, uint32_t* leaf_count, bool use_auction = false) {
+    if (n == 1) return bvh8(nodes, n, root, out, cap, prim_idx, node_count, leaf_count, use_auction);
+    std::vector<uint32_t> level = {root};  // BVH2 node of each BVH8 node of the level
+    uint32_t level_first = 0;              // BVH8 index of the level's first node
+    uint32_t node_ctr = 1, leaf_ctr = 0;
+    std::vector<CollapsedNode> col;
+    std::vector<uint32_t> cbase, pbase, next;
+    while (!level.empty()) {
+        const size_t m = level.size();
+        col.resize(m);
+        parallel_for(m, [&](size_t b, size_t e) {
+            for (size_t k = b; k < e; ++k) collapse_node(nodes, level[k], use_auction, col[k]);
+        }, 1024);
+        cbase.resize(m);
+        pbase.resize(m);
+        const uint32_t next_first = node_ctr;
+        for (size_t k = 0; k < m; ++k) {
+            const uint32_t ic = (uint32_t)__builtin_popcount(col[k].inner);
+            const uint32_t lc = (uint32_t)__builtin_popcount(col[k].leaf);
+            cbase[k] = node_ctr;
+            node_ctr += ic;
+            pbase[k] = lc ? leaf_ctr : 0;
+            leaf_ctr += lc;
+        }
+        if (node_ctr > cap) return 4;
+        if (leaf_ctr > n) return 2;
+        next.assign(node_ctr - next_first, kInvalid);
+        parallel_for(m, [&](size_t b, size_t e) {
+            for (size_t k = b; k < e; ++k) {
+                const CollapsedNode& c = col[k];
+                out[level_first + k] =
+                    make_node8(nodes[level[k]].b, c.child, cbase[k], pbase[k], c.asg, c.inner, c.leaf, nodes);
+                for (uint32_t i = 0; i < 8; ++i) {
+                    if (nib(c.asg, i) == 0xF) continue;
+                    const uint32_t ch = c.child[nib(c.asg, i)];
+                    if (c.inner & (1u << i))
+                        next[cbase[k] + below(c.inner, i) - next_first] = ch;
+                    else
+                        prim_idx[pbase[k] + below(c.leaf, i)] = nodes[ch].right;
+                }
+            }
+        }, 1024);
+        level.swap(next);
+        level_first = next_first;
+    }
+    *node_count = node_ctr;
+    *leaf_count = leaf_ctr;
+    return 0;
+}
+
 // ---------------------------------------------------------- cost
 // ComputeBVH2CostKernel (Eval.cu:12-33): internal C_T=3, leaf C_I=2.
 double bvh2_cost(const Node2* nodes, uint32_t count, const Box& root) {
@@ -821,6 +925,7 @@ bool same_box(const Box& a, const Box& b) { return std::memcmp(&a, &b, sizeof(Bo
 extern "C" {
 
 void orc_set_threads(int t) { g_threads = t; }
+void orc_set_level_collapse(int on) { g_level_collapse = on != 0; }
 int orc_get_threads(void) { return threads(); }
 void orc_set_area_form(int f) { g_area_form = f; }
 int orc_get_area_form(void) { return g_area_form; }
@@ -914,9 +1019,13 @@ int orc_bvh8(const void* bvh2_nodes, uint32_t n, uint32_t root, void* bvh8_nodes
              uint32_t* node_count, uint32_t* leaf_count) {
     return bvh8((const Node2*)bvh2_nodes, n, root, (Node8*)bvh8_nodes, cap, prim_idx, node_count, leaf_count);
 }
-// flags: 1 = auction slot assignment (NXB_BUILD_AUCTION).
+// flags: 1 = auction slot assignment (NXB_BUILD_AUCTION); 2 = the
+// level-parallel collapse (breadth-first numbering).
 int orc_bvh8_ex(const void* bvh2_nodes, uint32_t n, uint32_t root, void* bvh8_nodes, uint32_t cap,
                 uint32_t* prim_idx, uint32_t* node_count, uint32_t* leaf_count, uint32_t flags) {
+    if (flags & 2u)
+        return bvh8_levels((const Node2*)bvh2_nodes, n, root, (Node8*)bvh8_nodes, cap, prim_idx, node_count,
+                           leaf_count, (flags & 1u) != 0);
     return bvh8((const Node2*)bvh2_nodes, n, root, (Node8*)bvh8_nodes, cap, prim_idx, node_count, leaf_count,
                 (flags & 1u) != 0);
 }
@@ -1340,7 +1449,10 @@ int orc_build(const float* prims, int prim_type, uint32_t n, int key_bits, uint3
                       : hploc((const uint64_t*)sorted.data(), perm.data(), n, radius, nodes, &root);
     auto t4 = clk::now();
     uint32_t nc = 0, lc = 0;
-    if (bvh8_nodes) err |= bvh8(nodes, n, root, (Node8*)bvh8_nodes, bvh8_cap, prim_idx, &nc, &lc) << 8;
+    if (bvh8_nodes)
+        err |= (g_level_collapse ? bvh8_levels(nodes, n, root, (Node8*)bvh8_nodes, bvh8_cap, prim_idx, &nc, &lc)
+                                 : bvh8(nodes, n, root, (Node8*)bvh8_nodes, bvh8_cap, prim_idx, &nc, &lc))
+               << 8;
     auto t5 = clk::now();
     if (counts) {
         counts[0] = nc;

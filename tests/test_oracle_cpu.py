@@ -233,3 +233,30 @@ def test_auction_oracle_keeps_the_tree(orc):
     occupied = np.nonzero(bad[0]["meta"])[0][0]
     bad[0]["qhi"][1][occupied] ^= 1
     assert orc.compare_bvh8_unordered(bad, ap, g8, gp, 8000)[0] != 0
+
+
+@pytest.mark.parametrize("n,key_bits,boxes,auction", [(2, 30, False, False), (3, 63, False, False),
+                                                      (17, 30, True, False), (1000, 63, False, True),
+                                                      (65536, 30, False, False), (65536, 63, True, False)])
+def test_level_parallel_collapse_equals_the_work_slot_one(orc, n, key_bits, boxes, auction):
+    """The collapse timed as the CPU baseline builds the same BVH8 as the
+    parity oracle's (canonically: only node and primitive-slot numbering
+    differ), with the same node count and a valid, equally costly tree."""
+    prims = scenes.clustered(n, seed=n)
+    if boxes:
+        prims = scenes.to_boxes(prims)
+    r = orc.build(prims, key_bits)
+    a8, ap, ae = orc.bvh8(r["bvh2"], n, r["root"], auction=auction)
+    b8, bp, be = orc.bvh8(r["bvh2"], n, r["root"], auction=auction, levels=True)
+    assert ae == 0 and be == 0 and a8.shape == b8.shape
+    assert orc.compare_bvh8(b8, bp, a8, ap, n) == 0
+    assert orc.validate_bvh8(b8, bp, n, r["bvh2"][:n])[0] == 0
+    rb = np.concatenate([r["bvh2"][r["root"]]["bmin"], r["bvh2"][r["root"]]["bmax"]]).astype(np.float32)
+    assert abs(orc.bvh8_cost(b8, rb) - orc.bvh8_cost(a8, rb)) <= 1e-6 * orc.bvh8_cost(a8, rb)
+    # and through build(), where the CPU baseline uses it
+    orc.set_level_collapse(True)
+    try:
+        r2 = orc.build(prims, key_bits)
+    finally:
+        orc.set_level_collapse(False)
+    assert r2["err"] == 0 and orc.compare_bvh8(r2["bvh8"], r2["prim_idx"], r["bvh8"], r["prim_idx"], n) == 0
