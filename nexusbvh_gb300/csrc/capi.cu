@@ -63,8 +63,13 @@ Layout make_layout(uint32_t n, uint32_t key_bits) {
     Layout L;
     L.n = n;
     L.key_bytes = key_bits == 30 ? 4 : 8;
-    L.plan = key_bits == 30 ? make_sort_plan(2, 32) : make_sort_plan(1, 64);
-    L.tiles_words = sort_lookback_words(n, L.key_bytes, L.plan.passes);
+    // 30-bit keys: four 8-bit passes over [2,32); 63-bit keys: the hybrid
+    // sort (launch_sort63_hybrid), whose Morton-fused histograms are those of
+    // its four 9-bit top passes and whose look-back storage also serves its
+    // eight-pass fallback (the same number of words)
+    L.plan = key_bits == 30 ? make_sort_plan(2, 32) : hybrid63_top_plan();
+    L.tiles_words = key_bits == 30 ? sort_lookback_words(n, L.key_bytes, L.plan.passes)
+                                   : sort_lookback_words(n, L.key_bytes, kMaxSortPasses);
     size_t off = 0;
     auto seg = [&](size_t bytes) {
         size_t o = off;
@@ -166,18 +171,25 @@ nxb_status enqueue_build(const void* prims, nxb_prim_type type, uint32_t n, cons
     f.cluster_idx = nullptr;  // the first sort pass generates the values
     f.parent = parent;
     f.zero_ptr = lookback;
-    f.zero_words = align_up(4ull * L.tiles_words) / 4;
+    f.zero_words = align_up(4ull * L.tiles_words) / 4;  // both plans: the top passes' words, all of them
     f.scene_out = nullptr;
     f.seed_counters = true;
     NXB_TRY(launch_morton(bvh2, n, ctrl, (int)key_bits, keys_a, f, s));
     NXB_TRY(mark(2));
-    const size_t tiles_per_pass = L.tiles_words / L.plan.passes;
-    for (int p = 0; p < L.plan.passes; ++p) {
-        const bool even = (p % 2) == 0;
-        NXB_TRY(launch_sort_pass(L.key_bytes, even ? keys_a : keys_b, even ? keys_b : keys_a,
-                                 p == 0 ? nullptr : (even ? vals_a : vals_b), even ? vals_b : vals_a, n,
-                                 L.plan.shift[p], L.plan.bits[p], ctrl->hist[p], lookback + p * tiles_per_pass,
-                                 ctrl->tile_ctr + p, &ctrl->error_word, s));
+    if (key_bits == 30) {
+        const size_t tiles_per_pass = L.tiles_words / L.plan.passes;
+        for (int p = 0; p < L.plan.passes; ++p) {
+            const bool even = (p % 2) == 0;
+            NXB_TRY(launch_sort_pass(L.key_bytes, even ? keys_a : keys_b, even ? keys_b : keys_a,
+                                     p == 0 ? nullptr : (even ? vals_a : vals_b), even ? vals_b : vals_a, n,
+                                     L.plan.shift[p], L.plan.bits[p], ctrl->hist[p], lookback + p * tiles_per_pass,
+                                     ctrl->tile_ctr + p, &ctrl->error_word, s));
+        }
+    } else {
+        NXB_TRY(launch_sort63_hybrid(nullptr, nullptr, reinterpret_cast<uint64_t*>(keys_a),
+                                     reinterpret_cast<uint64_t*>(keys_b), vals_a, vals_b, n, &ctrl->hist[0][0], lookback,
+                                     ctrl->tile_ctr, &ctrl->sort_overflow, &ctrl->hist[0][0], &ctrl->fb_ticket,
+                                     ctrl->fb_done, &ctrl->error_word, s));
     }
     // an even number of passes leaves the sorted keys / permutation in A
     NXB_TRY(mark(3));
@@ -626,10 +638,22 @@ nxb_status nxb_stage_morton(const nxb_bvh2_node* d_nodes, uint32_t n, const nxb_
 }
 
 namespace {
+// 64-bit keys on the reference's 63-bit range [1,64) take the hybrid sort
+// (launch_sort63_hybrid); every other range the plain 8-bit passes.
+bool sort_is_hybrid(uint32_t key_bytes, uint32_t begin_bit, uint32_t end_bit) {
+    return key_bytes == 8 && begin_bit == 1 && end_bit == 64;
+}
+SortPlan sort_plan_of(uint32_t key_bytes, uint32_t begin_bit, uint32_t end_bit) {
+    return sort_is_hybrid(key_bytes, begin_bit, end_bit) ? hybrid63_top_plan() : make_sort_plan(begin_bit, end_bit);
+}
+
 struct SortScratch {
-    size_t hist, ctr, lookback, keys_tmp, vals_tmp, total;
+    size_t hist, ctr, hybrid, lookback, keys_tmp, vals_tmp, total;
 };
-SortScratch sort_scratch(uint32_t n, uint32_t key_bytes, const SortPlan& plan) {
+// hist | tile counters | hybrid words | look-back | keys | values; the
+// segments before keys_tmp are cleared by every call
+SortScratch sort_scratch(uint32_t n, uint32_t key_bytes, uint32_t begin_bit, uint32_t end_bit) {
+    const SortPlan plan = sort_plan_of(key_bytes, begin_bit, end_bit);
     SortScratch S{};
     size_t off = 0;
     auto seg = [&](size_t b) {
@@ -639,7 +663,11 @@ SortScratch sort_scratch(uint32_t n, uint32_t key_bytes, const SortPlan& plan) {
     };
     S.hist = seg(sizeof(uint32_t) * kMaxSortPasses * kRadixBins);
     S.ctr = seg(sizeof(uint32_t) * kMaxSortPasses);
-    S.lookback = seg(4ull * sort_lookback_words(n, key_bytes, plan.passes));
+    S.hybrid = seg(sizeof(uint32_t) * (kMaxSortPasses + 4));  // overflow, ticket, done[passes + 2]
+    // the hybrid's look-back serves its top passes and its 8-pass fallback
+    S.lookback = seg(4ull * (sort_is_hybrid(key_bytes, begin_bit, end_bit)
+                                 ? sort_lookback_words(n, key_bytes, kMaxSortPasses)
+                                 : sort_lookback_words(n, key_bytes, plan.passes)));
     S.keys_tmp = seg((size_t)key_bytes * n);
     S.vals_tmp = seg(4ull * n);
     S.total = off;
@@ -649,7 +677,7 @@ SortScratch sort_scratch(uint32_t n, uint32_t key_bytes, const SortPlan& plan) {
 
 size_t nxb_sort_scratch_bytes(uint32_t count, uint32_t key_bytes, uint32_t begin_bit, uint32_t end_bit) {
     if ((key_bytes != 4 && key_bytes != 8) || begin_bit >= end_bit || end_bit > key_bytes * 8) return 0;
-    return sort_scratch(count, key_bytes, make_sort_plan(begin_bit, end_bit)).total;
+    return sort_scratch(count, key_bytes, begin_bit, end_bit).total;
 }
 
 nxb_status nxb_stage_radix_sort(uint32_t key_bytes, const void* d_keys_in, void* d_keys_out,
@@ -660,8 +688,8 @@ nxb_status nxb_stage_radix_sort(uint32_t key_bytes, const void* d_keys_in, void*
     if (begin_bit >= end_bit || end_bit > key_bytes * 8) return NXB_ERR_INVALID_ARGUMENT;
     if (!d_keys_in || !d_keys_out || !d_vals_out || !d_scratch || n == 0) return NXB_ERR_INVALID_ARGUMENT;
     if (n > kMaxPrims) return NXB_ERR_UNSUPPORTED;
-    const SortPlan plan = make_sort_plan(begin_bit, end_bit);
-    const SortScratch S = sort_scratch(n, key_bytes, plan);
+    const SortPlan plan = sort_plan_of(key_bytes, begin_bit, end_bit);
+    const SortScratch S = sort_scratch(n, key_bytes, begin_bit, end_bit);
     if (scratch_bytes < S.total) return NXB_ERR_WORKSPACE_TOO_SMALL;
     unsigned char* base = (unsigned char*)d_scratch;
     uint32_t* hist = reinterpret_cast<uint32_t*>(base + S.hist);
@@ -669,6 +697,14 @@ nxb_status nxb_stage_radix_sort(uint32_t key_bytes, const void* d_keys_in, void*
     uint32_t* lookback = reinterpret_cast<uint32_t*>(base + S.lookback);
     NXB_TRY(cudaMemsetAsync(base, 0, S.keys_tmp, stream));
     NXB_TRY(launch_sort_histogram(key_bytes, d_keys_in, n, plan, hist, stream));
+    if (sort_is_hybrid(key_bytes, begin_bit, end_bit)) {
+        uint32_t* hy = reinterpret_cast<uint32_t*>(base + S.hybrid);
+        NXB_TRY(launch_sort63_hybrid(static_cast<const uint64_t*>(d_keys_in), d_vals_in,
+                                     static_cast<uint64_t*>(d_keys_out), reinterpret_cast<uint64_t*>(base + S.keys_tmp),
+                                     d_vals_out, reinterpret_cast<uint32_t*>(base + S.vals_tmp), n, hist, lookback, ctr,
+                                     hy, hist, hy + 1, hy + 2, d_error_word, stream));
+        return NXB_OK;
+    }
     const size_t per_pass = sort_lookback_words(n, key_bytes, 1);
     const void* kin = d_keys_in;
     const uint32_t* vin = d_vals_in;

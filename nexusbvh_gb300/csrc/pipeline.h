@@ -20,6 +20,11 @@ constexpr int kBvh8Claim = 0, kBvh8Nodes = 32, kBvh8Leaves = 64, kBvh8Alloc = 96
 constexpr int kBvh8CtrWords = 160;
 constexpr int kRadixBits = 8;
 constexpr int kRadixBins = 1 << kRadixBits;
+// Widest digit of a onesweep pass (the pipeline's 63-bit sort uses 9-bit
+// digits for its top passes; see launch_sort63_hybrid).
+constexpr int kMaxRadixBits = 9;
+// The 63-bit sort's top passes cover bits [kHybridTopShift, 64).
+constexpr uint32_t kHybridTopShift = 28;
 
 // Small per-build state, cleared by one memset at the start of a build.
 struct Control {
@@ -32,7 +37,12 @@ struct Control {
     uint32_t hploc_leaf_ctr; // H-PLOC: next unclaimed leaf
     uint32_t pad[2];
     uint32_t tile_ctr[kMaxSortPasses];
+    // histograms: kMaxSortPasses x 256 words, or 4 passes x 512 words of the
+    // 63-bit sort's top passes (the same storage)
     uint32_t hist[kMaxSortPasses][kRadixBins];
+    uint32_t sort_overflow;                // 63-bit sort: a bucket too large for shared memory
+    uint32_t fb_ticket;                    // 63-bit sort fallback: next ticket
+    uint32_t fb_done[kMaxSortPasses + 2];  // 63-bit sort fallback: finished tickets per stage
 };
 
 // Sort pass plan for the reference's bit ranges: [2,32) for 30-bit codes in
@@ -42,8 +52,24 @@ struct SortPlan {
     uint32_t shift[kMaxSortPasses];
     uint32_t bits[kMaxSortPasses];
 };
-// Passes of at most digit_bits (1..8) bits each, lowest digit first.
+// Passes of at most digit_bits (1..9) bits each, lowest digit first.
 SortPlan make_sort_plan(uint32_t begin_bit, uint32_t end_bit, uint32_t digit_bits = kRadixBits);
+// The top passes of the 63-bit sort: bits [kHybridTopShift, 64) in 9-bit digits.
+SortPlan hybrid63_top_plan();
+
+// The whole-array re-sort of the 63-bit sort (launch_sort63_hybrid): its
+// pass plan, look-back and histogram storage and ticket counters.
+struct SortFallback {
+    SortPlan plan;
+    uint32_t tiles;              // tiles per pass
+    uint32_t zero_tickets;       // tickets that clear the look-back words
+    uint32_t hist_tickets;       // tickets that count digits
+    size_t lookback_per_pass;    // words
+    uint32_t* lookback;
+    uint32_t* hist;              // plan.passes x 256 words
+    uint32_t* ticket;            // zero on entry
+    uint32_t* done;              // plan.passes + 2 words, zero on entry
+};
 
 struct DeviceInfo {
     int sms;
@@ -84,15 +110,31 @@ cudaError_t launch_morton(const Node2* nodes, uint32_t n, Control* ctrl, int key
 cudaError_t launch_morton_scene(const Node2* nodes, uint32_t n, const nxb_aabb* scene, int key_bits, void* keys,
                                 uint32_t* cluster_idx, cudaStream_t s);
 // ---------------------------------------------------------------- stage 3
-size_t sort_lookback_words(uint32_t n, uint32_t key_bytes, int passes);
+// Look-back words of `passes` passes with `bins` digits.
+size_t sort_lookback_words(uint32_t n, uint32_t key_bytes, int passes, uint32_t bins = kRadixBins);
 // Digit histograms of all passes (standalone sort only; the pipeline fuses
-// this into the Morton kernel).  hist must be zero on entry.
+// this into the Morton kernel), pass after pass, 1 << (widest digit of the
+// plan) words each.  hist must be zero on entry.
 cudaError_t launch_sort_histogram(uint32_t key_bytes, const void* keys, uint32_t n, const SortPlan& plan,
                                   uint32_t* hist, cudaStream_t s);
-// One onesweep pass.  vals_in == nullptr means values = input position.
+// One onesweep pass of `bits` <= 9 bits (9 only for 64-bit keys).
+// vals_in == nullptr means values = input position.
 cudaError_t launch_sort_pass(uint32_t key_bytes, const void* keys_in, void* keys_out, const uint32_t* vals_in,
                              uint32_t* vals_out, uint32_t n, uint32_t shift, uint32_t bits, const uint32_t* hist,
                              uint32_t* lookback, uint32_t* tile_ctr, uint32_t* err, cudaStream_t s);
+// The sort of 64-bit keys on bits [1,64) (the pipeline's 63-bit Morton
+// keys): four 9-bit passes over bits [28,64) (in -> B -> A -> B -> A;
+// top_hist = their 4 x 512 digit counts, lookback = their zeroed look-back
+// words, tile_ctr = 4 zeroed counters), the in-place sort of every bucket of
+// equal key >> 28, and the whole-array fallback, which runs only if a bucket
+// was too large (overflow, fb_ticket, fb_done zero on entry; it clears
+// fb_hist and lookback itself).  The first pass reads keys_in (keys_a if
+// null) and vals_in (the input positions if null); the sorted keys and the
+// permutation end in keys_a / vals_a.
+cudaError_t launch_sort63_hybrid(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_a, uint64_t* keys_b,
+                                 uint32_t* vals_a, uint32_t* vals_b, uint32_t n, const uint32_t* top_hist,
+                                 uint32_t* lookback, uint32_t* tile_ctr, uint32_t* overflow, uint32_t* fb_hist,
+                                 uint32_t* fb_ticket, uint32_t* fb_done, uint32_t* err, cudaStream_t s);
 // ---------------------------------------------------------------- stage 4
 // tokens: n words of scratch (no initialisation needed); parent_of_last:
 // one word that must hold INVALID on entry; leaf_ctr: one word that must

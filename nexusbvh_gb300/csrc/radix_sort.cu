@@ -44,9 +44,11 @@ __host__ __device__ constexpr int tile_keys() {
     return kThreads * Tile<K>::kKeysPerThread;
 }
 
-template <typename K>
+// Dynamic shared memory of a tile: its keys and values, then one digit
+// histogram per warp (RB-bit digits).
+template <typename K, int RB>
 __host__ __device__ constexpr size_t dyn_smem_bytes() {
-    return (size_t)tile_keys<K>() * (sizeof(K) + sizeof(uint32_t)) + (size_t)kWarps * kRadixBins * sizeof(uint32_t);
+    return (size_t)tile_keys<K>() * (sizeof(K) + sizeof(uint32_t)) + (size_t)kWarps * (1u << RB) * sizeof(uint32_t);
 }
 
 // Exclusive scan of one value per thread over a 256-thread CTA.
@@ -66,35 +68,60 @@ __device__ __forceinline__ uint32_t cta_exclusive_scan(uint32_t v, uint32_t* s_t
     return pre + incl - v;
 }
 
-template <typename K, bool HAS_VALS>
-__global__ __launch_bounds__(kThreads, 4) void onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout,
-                                                            const uint32_t* __restrict__ vin,
-                                                            uint32_t* __restrict__ vout, uint32_t n, uint32_t shift,
-                                                            uint32_t bits, const uint32_t* __restrict__ hist,
-                                                            uint32_t* lookback, uint32_t* tile_ctr, uint32_t* err) {
+template <bool L2, typename T>
+__device__ __forceinline__ T ld_data(const T* p) {
+    if constexpr (L2)
+        return __ldcg(p);
+    else
+        return *p;
+}
+
+// One onesweep tile: `bits`-bit digits at `shift` (bits <= RB), RB-bit
+// digit tables.  The caller has zeroed the per-warp histograms in the
+// dynamic shared memory and synchronised.  With RB = 9 each thread owns two
+// adjacent digits in the tile-wide steps (publish, look-back, scans).  L2:
+// every load of data written by other CTAs bypasses L1 (the persistent
+// fallback kernel reads buffers that other CTAs of the same launch wrote).
+template <typename K, bool HAS_VALS, int RB, bool L2>
+__device__ __forceinline__ void sort_tile(uint32_t tile, const K* __restrict__ kin, K* __restrict__ kout,
+                                          const uint32_t* __restrict__ vin, uint32_t* __restrict__ vout, uint32_t n,
+                                          uint32_t shift, uint32_t bits, const uint32_t* __restrict__ hist,
+                                          uint32_t* lookback, uint32_t* err, unsigned char* smem, uint32_t* s_delta,
+                                          uint16_t* s_local, uint32_t* s_tmp) {
     constexpr int KPT = Tile<K>::kKeysPerThread;
     constexpr int TILE = tile_keys<K>();
-    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int BINS = 1 << RB;
+    constexpr int DPT = BINS / kThreads;  // digits per thread: 1 or 2
+    static_assert(DPT == 1 || DPT == 2, "8- or 9-bit digit tables");
     K* s_keys = reinterpret_cast<K*>(smem);
     uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
     uint32_t* s_whist = s_vals + TILE;
-    __shared__ uint32_t s_local_start[kRadixBins];
-    __shared__ uint32_t s_global_start[kRadixBins];
-    __shared__ uint32_t s_tmp[kWarps];
-    __shared__ uint32_t s_tile;
 
     const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
     const uint32_t mask = (1u << bits) - 1u;
-    if (tid == 0) s_tile = atomicAdd(tile_ctr, 1u);
-    for (int i = tid; i < kWarps * kRadixBins; i += kThreads) s_whist[i] = 0;
-    __syncthreads();
-    const uint32_t tile = s_tile;
     const uint32_t tile_base = tile * (uint32_t)TILE;
     if (tile_base >= n) return;  // only reachable when a launch claims more tiles than exist
-    // global start of each digit (exclusive scan of this pass's histogram):
-    // only tile 0 needs it, the others inherit it through the look-back
-    uint32_t digit_base = 0;
-    if (tile == 0) digit_base = cta_exclusive_scan(tid <= mask ? hist[tid] : 0u, s_tmp);
+    const uint32_t d0 = tid * DPT;  // first digit this thread owns in the tile-wide steps
+    // the global start of each digit (exclusive scan of this pass's
+    // histogram): only tile 0 needs it, the others inherit it through the
+    // look-back
+    uint32_t excl[DPT];
+#pragma unroll
+    for (int k = 0; k < DPT; ++k) excl[k] = 0;
+    if (tile == 0) {
+        uint32_t h[DPT], hs = 0;
+#pragma unroll
+        for (int k = 0; k < DPT; ++k) {
+            h[k] = d0 + k <= mask ? ld_data<L2>(hist + d0 + k) : 0u;
+            hs += h[k];
+        }
+        uint32_t e = cta_exclusive_scan(hs, s_tmp);
+#pragma unroll
+        for (int k = 0; k < DPT; ++k) {
+            excl[k] = e;
+            e += h[k];
+        }
+    }
 
     // ---- load (warp-striped: warp w owns a contiguous run of 32*KPT keys)
     K key[KPT];
@@ -105,15 +132,15 @@ __global__ __launch_bounds__(kThreads, 4) void onesweep_kernel(const K* __restri
     for (int j = 0; j < KPT; ++j) {
         const uint32_t idx = wbase + 32u * j;
         const bool valid = idx < n;
-        key[j] = valid ? kin[idx] : (K)0;
+        key[j] = valid ? ld_data<L2>(kin + idx) : (K)0;
         if (HAS_VALS)
-            val[j] = valid ? vin[idx] : 0u;
+            val[j] = valid ? ld_data<L2>(vin + idx) : 0u;
         else
             val[j] = idx;
     }
 
     // ---- stable rank within the warp, one digit group at a time
-    uint32_t* wh = s_whist + warp * kRadixBins;
+    uint32_t* wh = s_whist + warp * BINS;
     const uint32_t lt_mask = lanemask_lt();
 #pragma unroll
     for (int j = 0; j < KPT; ++j) {
@@ -121,7 +148,7 @@ __global__ __launch_bounds__(kThreads, 4) void onesweep_kernel(const K* __restri
         const uint32_t d = (uint32_t)(key[j] >> shift) & mask;
         uint32_t peers = __ballot_sync(kFullMask, valid);
 #pragma unroll
-        for (int b = 0; b < kRadixBits; ++b) {
+        for (int b = 0; b < RB; ++b) {
             if (b < (int)bits) {
                 const bool bit = (d >> b) & 1u;
                 const uint32_t bb = __ballot_sync(kFullMask, bit);
@@ -141,28 +168,39 @@ __global__ __launch_bounds__(kThreads, 4) void onesweep_kernel(const K* __restri
     }
     __syncthreads();
 
-    // ---- per-digit tile count and per-warp exclusive offsets (thread = digit)
-    uint32_t tile_cnt = 0;
+    // ---- per-digit tile count and per-warp exclusive offsets (thread = digits d0 .. d0+DPT-1)
+    uint32_t cnt[DPT];
 #pragma unroll
-    for (int w = 0; w < kWarps; ++w) {
-        const uint32_t c = s_whist[w * kRadixBins + tid];
-        s_whist[w * kRadixBins + tid] = tile_cnt;
-        tile_cnt += c;
+    for (int k = 0; k < DPT; ++k) {
+        uint32_t c = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t x = s_whist[w * BINS + d0 + k];
+            s_whist[w * BINS + d0 + k] = c;
+            c += x;
+        }
+        cnt[k] = c;
     }
 
-    // ---- publish, then decoupled look-back for this digit
-    uint32_t* lb = lookback + (size_t)tile * kRadixBins;
-    uint32_t excl = 0;
-    if (tid <= mask) {
-        if (tile == 0) {
-            excl = digit_base;
-            atomicExch(lb + tid, kFlagInc | (excl + tile_cnt));
-        } else {
-            atomicExch(lb + tid, kFlagAgg | tile_cnt);
+    // ---- publish, then decoupled look-back for these digits
+    uint32_t* lb = lookback + (size_t)tile * BINS + d0;
+    const bool mine = d0 <= mask;  // digits beyond this pass's width are empty
+    if (tile == 0) {
+        if (mine) {
+            if constexpr (DPT == 1)
+                atomicExch(lb, kFlagInc | (excl[0] + cnt[0]));
+            else
+                st_relaxed_u64(reinterpret_cast<uint64_t*>(lb),
+                               (uint64_t)(kFlagInc | (excl[0] + cnt[0])) |
+                                   ((uint64_t)(kFlagInc | (excl[1] + cnt[1])) << 32));
+        }
+    } else if (mine) {
+        if constexpr (DPT == 1) {
+            atomicExch(lb, kFlagAgg | cnt[0]);
             int32_t pred = (int32_t)tile - 1;
             uint32_t polls = 0;
             while (pred >= 0) {
-                const uint32_t v = ld_relaxed_u32(lookback + (size_t)pred * kRadixBins + tid);
+                const uint32_t v = ld_relaxed_u32(lookback + (size_t)pred * BINS + d0);
                 const uint32_t flag = v & ~kCountMask;
                 if (flag == 0) {
                     if (++polls > kSpinLimit) {
@@ -172,15 +210,61 @@ __global__ __launch_bounds__(kThreads, 4) void onesweep_kernel(const K* __restri
                     if (polls > 64) __nanosleep(64);
                     continue;
                 }
-                excl += v & kCountMask;
+                excl[0] += v & kCountMask;
                 if (flag == kFlagInc) break;
                 --pred;
             }
-            atomicExch(lb + tid, kFlagInc | (excl + tile_cnt));
+            atomicExch(lb, kFlagInc | (excl[0] + cnt[0]));
+        } else {
+            // both digits' words in one 64-bit access; a digit stops adding
+            // once it has met an inclusive word
+            st_relaxed_u64(reinterpret_cast<uint64_t*>(lb),
+                           (uint64_t)(kFlagAgg | cnt[0]) | ((uint64_t)(kFlagAgg | cnt[1]) << 32));
+            int32_t pred = (int32_t)tile - 1;
+            uint32_t polls = 0;
+            bool done0 = false, done1 = false;
+            while (pred >= 0) {
+                const uint64_t v2 =
+                    ld_relaxed_u64(reinterpret_cast<const uint64_t*>(lookback + (size_t)pred * BINS + d0));
+                const uint32_t v0 = (uint32_t)v2, v1 = (uint32_t)(v2 >> 32);
+                const uint32_t f0 = v0 & ~kCountMask, f1 = v1 & ~kCountMask;
+                if ((!done0 && f0 == 0) || (!done1 && f1 == 0)) {
+                    if (++polls > kSpinLimit) {
+                        set_error(err, NXB_DEVERR_SORT_LOOKBACK_TIMEOUT);
+                        break;
+                    }
+                    if (polls > 64) __nanosleep(64);
+                    continue;
+                }
+                if (!done0) {
+                    excl[0] += v0 & kCountMask;
+                    done0 = f0 == kFlagInc;
+                }
+                if (!done1) {
+                    excl[1] += v1 & kCountMask;
+                    done1 = f1 == kFlagInc;
+                }
+                if (done0 && done1) break;
+                --pred;
+            }
+            st_relaxed_u64(reinterpret_cast<uint64_t*>(lb), (uint64_t)(kFlagInc | (excl[0] + cnt[0])) |
+                                                                 ((uint64_t)(kFlagInc | (excl[1] + cnt[1])) << 32));
         }
     }
-    s_global_start[tid] = excl;
-    s_local_start[tid] = cta_exclusive_scan(tid <= mask ? tile_cnt : 0u, s_tmp);
+    // local start of each digit in the tile (s_local), and the offset that
+    // maps a tile position to its global position (s_delta)
+    {
+        uint32_t cs = 0;
+#pragma unroll
+        for (int k = 0; k < DPT; ++k) cs += d0 + k <= mask ? cnt[k] : 0u;
+        uint32_t e = cta_exclusive_scan(cs, s_tmp);
+#pragma unroll
+        for (int k = 0; k < DPT; ++k) {
+            s_local[d0 + k] = (uint16_t)e;
+            s_delta[d0 + k] = excl[k] - e;
+            e += cnt[k];
+        }
+    }
     __syncthreads();
 
     // ---- reorder the tile by digit in shared memory
@@ -188,7 +272,7 @@ __global__ __launch_bounds__(kThreads, 4) void onesweep_kernel(const K* __restri
     for (int j = 0; j < KPT; ++j) {
         if (wbase + 32u * j < n) {
             const uint32_t d = (uint32_t)(key[j] >> shift) & mask;
-            const uint32_t pos = s_local_start[d] + wh[d] + rank[j];
+            const uint32_t pos = s_local[d] + wh[d] + rank[j];
             s_keys[pos] = key[j];
             s_vals[pos] = val[j];
         }
@@ -200,7 +284,7 @@ __global__ __launch_bounds__(kThreads, 4) void onesweep_kernel(const K* __restri
     for (uint32_t i = tid; i < tile_n; i += kThreads) {
         const K k = s_keys[i];
         const uint32_t d = (uint32_t)(k >> shift) & mask;
-        const uint32_t g = s_global_start[d] + (i - s_local_start[d]);
+        const uint32_t g = s_delta[d] + i;
         if (g < n) {  // always true unless a look-back wait expired
             kout[g] = k;
             vout[g] = s_vals[i];
@@ -208,28 +292,346 @@ __global__ __launch_bounds__(kThreads, 4) void onesweep_kernel(const K* __restri
     }
 }
 
-template <typename K>
+template <typename K, bool HAS_VALS, int RB>
+__global__ __launch_bounds__(kThreads, 4) void onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout,
+                                                            const uint32_t* __restrict__ vin,
+                                                            uint32_t* __restrict__ vout, uint32_t n, uint32_t shift,
+                                                            uint32_t bits, const uint32_t* __restrict__ hist,
+                                                            uint32_t* lookback, uint32_t* tile_ctr, uint32_t* err) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ uint32_t s_delta[1 << RB];
+    __shared__ uint16_t s_local[1 << RB];
+    __shared__ uint32_t s_tmp[kWarps];
+    __shared__ uint32_t s_tile;
+    uint32_t* s_whist = reinterpret_cast<uint32_t*>(smem + (size_t)tile_keys<K>() * (sizeof(K) + sizeof(uint32_t)));
+    if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr, 1u);
+    for (int i = threadIdx.x; i < kWarps * (1 << RB); i += kThreads) s_whist[i] = 0;
+    __syncthreads();
+    sort_tile<K, HAS_VALS, RB, false>(s_tile, kin, kout, vin, vout, n, shift, bits, hist, lookback, err, smem, s_delta,
+                                      s_local, s_tmp);
+}
+
+// Runs `set` (kernel attribute calls) once per device, with that device
+// current, from any number of host threads; later calls return its result.
+// Each call site passes its own lambda type and so has its own flags.
+template <typename F>
+cudaError_t once_per_device(F set) {
+    constexpr int kMaxDev = 64;
+    static std::once_flag once[kMaxDev];
+    static cudaError_t result[kMaxDev];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
+    std::call_once(once[dev], [&] { result[dev] = set(); });
+    return result[dev];
+}
+
+// Dynamic shared memory above the 48 KB default (the 9-bit tables) and the
+// carveout for four tiles per SM: shared memory, not L1.
+template <typename Kern>
+cudaError_t set_smem_attributes(Kern* kernel, size_t bytes) {
+    cudaError_t r = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (!r) r = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    return r;
+}
+
+template <typename K, int RB>
+cudaError_t configure_onesweep() {
+    return once_per_device([] {
+        constexpr size_t smem = dyn_smem_bytes<K, RB>();
+        cudaError_t r = set_smem_attributes(onesweep_kernel<K, true, RB>, smem);
+        if (!r) r = set_smem_attributes(onesweep_kernel<K, false, RB>, smem);
+        return r;
+    });
+}
+
+template <typename K, int RB>
 cudaError_t launch_pass_t(const K* kin, K* kout, const uint32_t* vin, uint32_t* vout, uint32_t n, uint32_t shift,
                           uint32_t bits, const uint32_t* hist, uint32_t* lookback, uint32_t* tile_ctr, uint32_t* err,
                           cudaStream_t s) {
-    constexpr size_t smem = dyn_smem_bytes<K>();
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(onesweep_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(onesweep_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        // four tiles per SM: shared memory, not L1, gets the carveout
-        cudaFuncSetAttribute(onesweep_kernel<K, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        cudaFuncSetAttribute(onesweep_kernel<K, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        configured = true;
-    }
+    constexpr size_t smem = dyn_smem_bytes<K, RB>();
+    cudaError_t e = configure_onesweep<K, RB>();
+    if (e != cudaSuccess) return e;
     const uint32_t tiles = (n + tile_keys<K>() - 1) / tile_keys<K>();
     if (vin)
-        onesweep_kernel<K, true><<<tiles, kThreads, smem, s>>>(kin, kout, vin, vout, n, shift, bits, hist, lookback,
-                                                              tile_ctr, err);
+        onesweep_kernel<K, true, RB><<<tiles, kThreads, smem, s>>>(kin, kout, vin, vout, n, shift, bits, hist,
+                                                                  lookback, tile_ctr, err);
     else
-        onesweep_kernel<K, false><<<tiles, kThreads, smem, s>>>(kin, kout, vin, vout, n, shift, bits, hist, lookback,
-                                                               tile_ctr, err);
+        onesweep_kernel<K, false, RB><<<tiles, kThreads, smem, s>>>(kin, kout, vin, vout, n, shift, bits, hist,
+                                                                   lookback, tile_ctr, err);
     return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- bucket sort
+// The pipeline sorts 63-bit Morton keys on bits [1,64) (Setup.cu:74-78) in
+// two steps.  Four 9-bit onesweep passes sort them stably on bits [28,64);
+// that groups the keys into buckets of equal key >> 28 (a cell of the Morton
+// order 12 levels deep), which on meshes hold a handful of keys each.  Then
+// bucket_sort_kernel sorts every bucket in place, stably, on bits [1,28)
+// inside shared memory.  Keys equal on bits [1,64) keep their input order
+// through both steps, so the result is exactly the stable sort of the whole
+// range.  A bucket larger than kBucketCap is not sorted here: the kernel
+// raises the overflow word and sort_fallback_kernel then sorts the whole
+// array again with the plain eight 8-bit passes (a stable sort of an array
+// in which equal keys are still in input order gives the same permutation).
+constexpr uint32_t kBucketWindow = 2048;  // buckets owned by one CTA start in its window
+constexpr uint32_t kBucketCap = 1024;     // largest bucket sorted in shared memory
+constexpr uint32_t kBucketSlots = kBucketWindow + kBucketCap;
+constexpr int kBucketThreads = 256;
+constexpr int kBucketPer = kBucketSlots / kBucketThreads;
+static_assert(kBucketSlots % kBucketThreads == 0, "whole slots per thread");
+static_assert(kBucketSlots <= 0xFFFFu, "16-bit bucket bounds");
+constexpr size_t kBucketSmem = (size_t)kBucketSlots * (8 + 4 + 4 + 2 + 2);
+
+// One CTA per window of kBucketWindow positions: it owns the buckets that
+// start in its window (the last one may run on past the window, into at
+// most kBucketCap more positions), sorts each of them by its rank and
+// writes the keys that move.  Other CTAs only read the top bits of keys
+// outside their own buckets, which a permutation inside a bucket does not
+// change, so the sort runs in place.
+__global__ __launch_bounds__(kBucketThreads) void bucket_sort_kernel(uint64_t* keys, uint32_t* vals, uint32_t n,
+                                                                     uint32_t top_shift, uint32_t begin_bit,
+                                                                     uint32_t* overflow) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint64_t* s_key = reinterpret_cast<uint64_t*>(smem);
+    uint32_t* s_val = reinterpret_cast<uint32_t*>(s_key + kBucketSlots);
+    uint32_t* s_cmp = s_val + kBucketSlots;
+    uint16_t* s_bs = reinterpret_cast<uint16_t*>(s_cmp + kBucketSlots);
+    uint16_t* s_be = s_bs + kBucketSlots;
+    __shared__ uint32_t s_first, s_len, s_open;
+    __shared__ int32_t s_wmax[kBucketThreads / 32];
+    __shared__ uint32_t s_wmin[kBucketThreads / 32];
+
+    const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
+    const uint32_t w0 = blockIdx.x * kBucketWindow;
+    const uint32_t wn = min(kBucketWindow, n - w0);
+    const uint64_t cmp_mask = (1ull << (top_shift - begin_bit)) - 1ull;
+    if (tid == 0) {
+        s_first = kInvalid;
+        s_len = wn;
+        s_open = 0;
+    }
+    for (uint32_t j = tid; j < wn; j += kBucketThreads) {
+        const uint64_t k = __ldcg(keys + w0 + j);
+        s_key[j] = k;
+        s_val[j] = __ldcg(vals + w0 + j);
+        s_cmp[j] = (uint32_t)((k >> begin_bit) & cmp_mask);
+    }
+    __syncthreads();
+    // the first bucket start of the window
+    for (uint32_t j = tid; j < wn; j += kBucketThreads) {
+        const bool start = j == 0 ? (w0 == 0 || (__ldcg(keys + w0 - 1) >> top_shift) != (s_key[0] >> top_shift))
+                                  : (s_key[j] >> top_shift) != (s_key[j - 1] >> top_shift);
+        if (start) {
+            atomicMin(&s_first, j);
+            break;  // a thread's later positions are larger
+        }
+    }
+    __syncthreads();
+    const uint32_t s0 = s_first;
+    if (s0 == kInvalid) return;  // the window lies inside a bucket that started earlier
+    // the rest of the window's last bucket, past the window (warp 0)
+    if (warp == 0 && w0 + wn < n) {
+        const uint64_t last = s_key[wn - 1] >> top_shift;
+        uint32_t len = wn;
+        for (;;) {
+            const uint32_t g = w0 + len + lane;
+            const bool in = g < n && len + lane < kBucketSlots;
+            uint64_t k = 0;
+            if (in) k = __ldcg(keys + g);
+            const uint32_t stop = __ballot_sync(kFullMask, !in || (k >> top_shift) != last);
+            const uint32_t take = stop ? (uint32_t)(__ffs(stop) - 1) : 32u;
+            if (lane < take) {
+                s_key[len + lane] = k;
+                s_val[len + lane] = __ldcg(vals + g);
+                s_cmp[len + lane] = (uint32_t)((k >> begin_bit) & cmp_mask);
+            }
+            len += take;
+            if (!stop) continue;
+            // stopped at a new bucket, at the end of the keys, or with the
+            // slots full inside the bucket
+            if (len >= kBucketSlots && w0 + len < n && lane == 0 && (__ldcg(keys + w0 + len) >> top_shift) == last)
+                s_open = 1;
+            break;
+        }
+        if (lane == 0) s_len = len;
+    }
+    __syncthreads();
+    const uint32_t len = s_len;
+    if (s_open) {  // the last bucket is larger than the slots: leave everything to the fallback
+        if (tid == 0) atomicOr(overflow, 1u);
+        return;
+    }
+    // bucket bounds: bs = the last start <= j, be = the first start > j
+    // (or len), by a forward max-scan and a backward min-scan over blocked
+    // ranges of kBucketPer positions per thread
+    const uint32_t j0 = tid * kBucketPer;
+    auto is_start = [&](uint32_t j) -> bool {
+        return j == 0 ? s0 == 0 : (s_key[j] >> top_shift) != (s_key[j - 1] >> top_shift);
+    };
+    int32_t lbs[kBucketPer];
+    uint32_t lbe[kBucketPer];
+    int32_t cur = -1;
+#pragma unroll
+    for (int k = 0; k < kBucketPer; ++k) {
+        const uint32_t j = j0 + k;
+        if (j < len && is_start(j)) cur = (int32_t)j;
+        lbs[k] = cur;
+    }
+    uint32_t nxt = len;
+#pragma unroll
+    for (int k = kBucketPer - 1; k >= 0; --k) {
+        const uint32_t j = j0 + k;
+        lbe[k] = nxt;
+        if (j < len && is_start(j)) nxt = j;
+    }
+    // exclusive max-scan of cur over the threads before, min-scan of nxt over the threads after
+    int32_t incl_max = cur;
+    uint32_t incl_min = nxt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int32_t y = __shfl_up_sync(kFullMask, incl_max, o);
+        if (lane >= (uint32_t)o) incl_max = max(incl_max, y);
+        const uint32_t z = __shfl_down_sync(kFullMask, incl_min, o);
+        if (lane + o < 32u) incl_min = min(incl_min, z);
+    }
+    if (lane == 31) s_wmax[warp] = incl_max;
+    if (lane == 0) s_wmin[warp] = incl_min;
+    __syncthreads();
+    int32_t before = __shfl_up_sync(kFullMask, incl_max, 1);
+    if (lane == 0) before = -1;
+    uint32_t after = __shfl_down_sync(kFullMask, incl_min, 1);
+    if (lane == 31) after = len;
+    for (uint32_t w = 0; w < warp; ++w) before = max(before, s_wmax[w]);
+    for (uint32_t w = warp + 1; w < kBucketThreads / 32; ++w) after = min(after, s_wmin[w]);
+#pragma unroll
+    for (int k = 0; k < kBucketPer; ++k) {
+        const uint32_t j = j0 + k;
+        if (j < len) {
+            s_bs[j] = (uint16_t)max(lbs[k] >= 0 ? lbs[k] : before, 0);
+            s_be[j] = (uint16_t)(lbe[k] < len ? lbe[k] : after);
+        }
+    }
+    __syncthreads();
+    // rank of each key in its bucket: keys below it, and equal keys before it
+    bool over = false;
+    for (uint32_t j = s0 + tid; j < len; j += kBucketThreads) {
+        const uint32_t bs = s_bs[j], be = s_be[j];
+        if (be - bs > kBucketCap) {
+            over = true;
+            continue;
+        }
+        if (be - bs == 1) continue;
+        const uint32_t c = s_cmp[j];
+        uint32_t r = 0;
+        for (uint32_t i = bs; i < be; ++i) {
+            const uint32_t ci = s_cmp[i];
+            r += (ci < c || (ci == c && i < j)) ? 1u : 0u;
+        }
+        const uint32_t dst = bs + r;
+        if (dst != j) {
+            keys[w0 + dst] = s_key[j];
+            vals[w0 + dst] = s_val[j];
+        }
+    }
+    if (over) atomicOr(overflow, 1u);
+}
+
+// ---------------------------------------------------------------- fallback
+// The whole-array re-sort of the bucket overflow case as ONE persistent
+// launch that does nothing when the overflow word is clear.  Its work is a
+// sequence of tickets claimed in order from one counter: clearing the
+// look-back words and histograms, counting the digits of every pass, then
+// the tiles of pass 0, 1, ...  A ticket whose stage needs the previous
+// stage complete waits (bounded) on that stage's done counter; every
+// ticket it waits on was claimed earlier by a running CTA, which only
+// waits on tickets claimed before its own, so the waits always end.
+constexpr uint32_t kFbZeroWords = 1u << 16;  // look-back words cleared per ticket
+constexpr uint32_t kFbHistKeys = 1u << 14;   // keys counted per ticket
+
+template <typename K>
+__global__ __launch_bounds__(kThreads, 4) void sort_fallback_kernel(K* ka, K* kb, uint32_t* va, uint32_t* vb,
+                                                                   uint32_t n, const uint32_t* overflow,
+                                                                   SortFallback f, uint32_t* err) {
+    if (ld_relaxed_u32(overflow) == 0) return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ uint32_t s_delta[kRadixBins];
+    __shared__ uint16_t s_local[kRadixBins];
+    __shared__ uint32_t s_tmp[kWarps];
+    __shared__ uint32_t s_ticket, s_ok;
+    uint32_t* s_whist = reinterpret_cast<uint32_t*>(smem + (size_t)tile_keys<K>() * (sizeof(K) + sizeof(uint32_t)));
+    const uint32_t passes = (uint32_t)f.plan.passes;
+    const uint32_t total = f.zero_tickets + f.hist_tickets + passes * f.tiles;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_ticket = atomicAdd(f.ticket, 1u);
+        for (int i = threadIdx.x; i < kWarps * kRadixBins; i += kThreads) s_whist[i] = 0;
+        __syncthreads();
+        const uint32_t t = s_ticket;
+        if (t >= total) return;
+        uint32_t stage, local, wait_stage = 0, wait_for = 0;
+        if (t < f.zero_tickets) {
+            stage = 0;
+            local = t;
+        } else if (t < f.zero_tickets + f.hist_tickets) {
+            stage = 1;
+            local = t - f.zero_tickets;
+            wait_stage = 0;
+            wait_for = f.zero_tickets;
+        } else {
+            const uint32_t q = t - f.zero_tickets - f.hist_tickets;
+            const uint32_t p = q / f.tiles;
+            stage = 2 + p;
+            local = q - p * f.tiles;
+            wait_stage = stage - 1;
+            wait_for = p == 0 ? f.hist_tickets : f.tiles;
+        }
+        if (threadIdx.x == 0) {
+            uint32_t ok = 1, polls = 0;
+            if (stage > 0) {
+                while (ld_acquire_u32(f.done + wait_stage) < wait_for) {
+                    if (++polls > kSpinLimit) {
+                        set_error(err, NXB_DEVERR_SORT_LOOKBACK_TIMEOUT);
+                        ok = 0;
+                        break;
+                    }
+                    __nanosleep(polls > 64 ? 256 : 32);
+                }
+            }
+            s_ok = ok;
+        }
+        __syncthreads();
+        if (!s_ok) return;
+        if (stage == 0) {
+            const size_t words = f.lookback_per_pass * passes;
+            const size_t b = (size_t)local * kFbZeroWords, e = min(words, b + kFbZeroWords);
+            for (size_t w = b + threadIdx.x; w < e; w += kThreads) f.lookback[w] = 0;
+            if (local == 0)
+                for (uint32_t i = threadIdx.x; i < passes * kRadixBins; i += kThreads) f.hist[i] = 0;
+        } else if (stage == 1) {
+            const uint32_t b = local * kFbHistKeys, e = min(n, b + kFbHistKeys);
+            for (uint32_t i = b + threadIdx.x; i < e; i += kThreads) {
+                const K k = __ldcg(ka + i);
+                for (uint32_t p = 0; p < passes; ++p)
+                    atomicAdd(&s_whist[p * kRadixBins + ((uint32_t)(k >> f.plan.shift[p]) & ((1u << f.plan.bits[p]) - 1u))],
+                              1u);
+            }
+            __syncthreads();
+            for (uint32_t i = threadIdx.x; i < passes * kRadixBins; i += kThreads)
+                if (s_whist[i]) atomicAdd(f.hist + i, s_whist[i]);
+        } else {
+            const uint32_t p = stage - 2;
+            const bool even = (p & 1u) == 0;
+            sort_tile<K, true, kRadixBits, true>(local, even ? ka : kb, even ? kb : ka, even ? va : vb, even ? vb : va,
+                                                 n, f.plan.shift[p], f.plan.bits[p], f.hist + p * kRadixBins,
+                                                 f.lookback + (size_t)p * f.lookback_per_pass, err, smem, s_delta,
+                                                 s_local, s_tmp);
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) atomicAdd(f.done + stage, 1u);
+    }
 }
 
 }  // namespace
@@ -253,12 +655,11 @@ cudaError_t run_sort_stall_probe(uint32_t* err_out) {
     e = cudaMemset(buf, 0, bytes);
     const uint32_t one = 1;
     if (!e) e = cudaMemcpy(ctr, &one, 4, cudaMemcpyHostToDevice);
-    constexpr size_t smem = dyn_smem_bytes<uint32_t>();
-    if (!e) e = cudaFuncSetAttribute(onesweep_kernel<uint32_t, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem);
+    constexpr size_t smem = dyn_smem_bytes<uint32_t, kRadixBits>();
+    if (!e) e = configure_onesweep<uint32_t, kRadixBits>();
     if (!e) {
-        onesweep_kernel<uint32_t, false><<<1, kThreads, smem>>>(keys, kout, nullptr, vout, n, 0, 8, hist, lookback,
-                                                                 ctr, err);
+        onesweep_kernel<uint32_t, false, kRadixBits><<<1, kThreads, smem>>>(keys, kout, nullptr, vout, n, 0, 8, hist,
+                                                                            lookback, ctr, err);
         e = cudaGetLastError();
     }
     if (!e) e = cudaMemcpy(err_out, err, 4, cudaMemcpyDeviceToHost);
@@ -268,7 +669,7 @@ cudaError_t run_sort_stall_probe(uint32_t* err_out) {
 
 SortPlan make_sort_plan(uint32_t begin_bit, uint32_t end_bit, uint32_t digit_bits) {
     SortPlan p{};
-    digit_bits = std::max(1u, std::min<uint32_t>(digit_bits, kRadixBits));
+    digit_bits = std::max(1u, std::min<uint32_t>(digit_bits, kMaxRadixBits));
     for (uint32_t b = begin_bit; b < end_bit && p.passes < kMaxSortPasses; b += digit_bits) {
         p.shift[p.passes] = b;
         p.bits[p.passes] = std::min<uint32_t>(digit_bits, end_bit - b);
@@ -277,20 +678,75 @@ SortPlan make_sort_plan(uint32_t begin_bit, uint32_t end_bit, uint32_t digit_bit
     return p;
 }
 
-size_t sort_lookback_words(uint32_t n, uint32_t key_bytes, int passes) {
+SortPlan hybrid63_top_plan() { return make_sort_plan(kHybridTopShift, 64, kMaxRadixBits); }
+
+size_t sort_lookback_words(uint32_t n, uint32_t key_bytes, int passes, uint32_t bins) {
     uint32_t tk = key_bytes == 4 ? tile_keys<uint32_t>() : tile_keys<uint64_t>();
     size_t tiles = (n + tk - 1) / tk;
-    return tiles * kRadixBins * (size_t)passes;
+    return tiles * bins * (size_t)passes;
 }
 
 cudaError_t launch_sort_pass(uint32_t key_bytes, const void* keys_in, void* keys_out, const uint32_t* vals_in,
                              uint32_t* vals_out, uint32_t n, uint32_t shift, uint32_t bits, const uint32_t* hist,
                              uint32_t* lookback, uint32_t* tile_ctr, uint32_t* err, cudaStream_t s) {
-    if (key_bytes == 4)
-        return launch_pass_t<uint32_t>((const uint32_t*)keys_in, (uint32_t*)keys_out, vals_in, vals_out, n, shift,
-                                       bits, hist, lookback, tile_ctr, err, s);
-    return launch_pass_t<uint64_t>((const uint64_t*)keys_in, (uint64_t*)keys_out, vals_in, vals_out, n, shift, bits,
-                                   hist, lookback, tile_ctr, err, s);
+    if (key_bytes == 4) {
+        if (bits > kRadixBits) return cudaErrorInvalidValue;
+        return launch_pass_t<uint32_t, kRadixBits>((const uint32_t*)keys_in, (uint32_t*)keys_out, vals_in, vals_out, n,
+                                                   shift, bits, hist, lookback, tile_ctr, err, s);
+    }
+    if (bits > kRadixBits)
+        return launch_pass_t<uint64_t, kMaxRadixBits>((const uint64_t*)keys_in, (uint64_t*)keys_out, vals_in, vals_out,
+                                                      n, shift, bits, hist, lookback, tile_ctr, err, s);
+    return launch_pass_t<uint64_t, kRadixBits>((const uint64_t*)keys_in, (uint64_t*)keys_out, vals_in, vals_out, n,
+                                               shift, bits, hist, lookback, tile_ctr, err, s);
+}
+
+cudaError_t launch_sort63_hybrid(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_a, uint64_t* keys_b,
+                                 uint32_t* vals_a, uint32_t* vals_b, uint32_t n, const uint32_t* top_hist,
+                                 uint32_t* lookback, uint32_t* tile_ctr, uint32_t* overflow, uint32_t* fb_hist,
+                                 uint32_t* fb_ticket, uint32_t* fb_done, uint32_t* err, cudaStream_t s) {
+    const SortPlan top = hybrid63_top_plan();
+    constexpr uint32_t kTopBins = 1u << kMaxRadixBits;
+    const size_t top_words = sort_lookback_words(n, 8, 1, kTopBins);
+    // even pass count: the keys end in A
+    for (int p = 0; p < top.passes; ++p) {
+        const bool even = (p % 2) == 0;
+        const uint64_t* kin = p == 0 && keys_in ? keys_in : (even ? keys_a : keys_b);
+        const uint32_t* vin = p == 0 ? vals_in : (even ? vals_a : vals_b);
+        cudaError_t e = launch_sort_pass(8, kin, even ? keys_b : keys_a, vin, even ? vals_b : vals_a, n,
+                                         top.shift[p], top.bits[p], top_hist + p * kTopBins, lookback + p * top_words,
+                                         tile_ctr + p, err, s);
+        if (e != cudaSuccess) return e;
+    }
+    {
+        cudaError_t attr = once_per_device([] {
+            return cudaFuncSetAttribute(bucket_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)kBucketSmem);
+        });
+        if (attr != cudaSuccess) return attr;
+        const uint32_t windows = (n + kBucketWindow - 1) / kBucketWindow;
+        bucket_sort_kernel<<<windows, kBucketThreads, kBucketSmem, s>>>(keys_a, vals_a, n, kHybridTopShift, 1,
+                                                                         overflow);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    SortFallback f{};
+    f.plan = make_sort_plan(1, 64);
+    f.tiles = (n + tile_keys<uint64_t>() - 1) / tile_keys<uint64_t>();
+    f.lookback_per_pass = sort_lookback_words(n, 8, 1, kRadixBins);
+    f.zero_tickets = (uint32_t)((f.lookback_per_pass * f.plan.passes + kFbZeroWords - 1) / kFbZeroWords);
+    f.hist_tickets = (n + kFbHistKeys - 1) / kFbHistKeys;
+    f.lookback = lookback;
+    f.hist = fb_hist;
+    f.ticket = fb_ticket;
+    f.done = fb_done;
+    constexpr size_t smem = dyn_smem_bytes<uint64_t, kRadixBits>();
+    cudaError_t e = once_per_device([] { return set_smem_attributes(sort_fallback_kernel<uint64_t>, smem); });
+    if (e != cudaSuccess) return e;
+    const uint32_t total = f.zero_tickets + f.hist_tickets + (uint32_t)f.plan.passes * f.tiles;
+    const uint32_t grid = std::max(1u, std::min(total, (uint32_t)device_info().sms * 4u));
+    sort_fallback_kernel<uint64_t><<<grid, kThreads, smem, s>>>(keys_a, keys_b, vals_a, vals_b, n, overflow, f, err);
+    return cudaGetLastError();
 }
 
 }  // namespace nxb

@@ -148,11 +148,14 @@ struct MortonArgs {
     int seed;
 };
 
-// PASSES > 0: the pass count of the plan, known at compile time (8 for
-// 63-bit keys, 4 for 30-bit), so the histogram loop unrolls.
-template <typename K, bool HIST, int PASSES = 0>
+// PASSES > 0: the pass count of the plan, known at compile time (4 for
+// 30-bit keys, 4 for the 9-bit top passes of 63-bit keys), so the histogram
+// loop unrolls.  BINS: digits per pass (256, or 512 for 9-bit digits); the
+// histograms are laid out pass after pass, BINS words each.
+template <typename K, bool HIST, int PASSES = 0, int BINS = kRadixBins>
 __global__ __launch_bounds__(kThreads) void morton_kernel(const Node2* __restrict__ nodes, uint32_t n, Control* ctrl,
                                                           K* __restrict__ keys, MortonArgs a) {
+    static_assert(PASSES * BINS <= kMaxSortPasses * kRadixBins, "histograms fit the control block");
     __shared__ float s_scene[6];
     __shared__ uint32_t s_hist[HIST ? kMaxSortPasses * kRadixBins : 1];
     if (threadIdx.x < 6) {
@@ -160,7 +163,7 @@ __global__ __launch_bounds__(kThreads) void morton_kernel(const Node2* __restric
         s_scene[threadIdx.x] = ord2f(threadIdx.x < 3 ? ~o : o);
     }
     if (HIST)
-        for (int i = threadIdx.x; i < a.pd.passes * kRadixBins; i += kThreads) s_hist[i] = 0;
+        for (int i = threadIdx.x; i < a.pd.passes * BINS; i += kThreads) s_hist[i] = 0;
     __syncthreads();
     const float3 smin = make_float3(s_scene[0], s_scene[1], s_scene[2]);
     const float3 smax = make_float3(s_scene[3], s_scene[4], s_scene[5]);
@@ -204,16 +207,16 @@ __global__ __launch_bounds__(kThreads) void morton_kernel(const Node2* __restric
                     if (p < PASSES / 2) {
                         // low digits: neighbouring keys rarely share them,
                         // so the warp-uniform test seldom pays for itself
-                        if (valid) atomicAdd(&s_hist[p * kRadixBins + d], 1u);
+                        if (valid) atomicAdd(&s_hist[p * BINS + d], 1u);
                     } else {
-                        hist_add(s_hist + p * kRadixBins, d, valid);
+                        hist_add(s_hist + p * BINS, d, valid);
                     }
                 }
             } else {
 #pragma unroll 1
                 for (int p = 0; p < a.pd.passes; ++p) {
                     uint32_t d = (uint32_t)(key >> a.pd.shift[p]) & a.pd.mask[p];
-                    hist_add(s_hist + p * kRadixBins, d, valid);
+                    hist_add(s_hist + p * BINS, d, valid);
                 }
             }
         }
@@ -224,7 +227,7 @@ __global__ __launch_bounds__(kThreads) void morton_kernel(const Node2* __restric
         a.ones_ptr[w] = make_uint4(kInvalid, kInvalid, kInvalid, kInvalid);
     if (HIST) {
         __syncthreads();
-        for (int i = threadIdx.x; i < a.pd.passes * kRadixBins; i += kThreads)
+        for (int i = threadIdx.x; i < a.pd.passes * BINS; i += kThreads)
             if (s_hist[i]) atomicAdd(&ctrl->hist[0][0] + i, s_hist[i]);
     }
 }
@@ -241,11 +244,12 @@ __global__ __launch_bounds__(kThreads) void morton_scene_kernel(const Node2* __r
     }
 }
 
+// bins: histogram words per pass (1 << the plan's widest digit).
 template <typename K>
 __global__ __launch_bounds__(kThreads) void sort_histogram_kernel(const K* __restrict__ keys, uint32_t n,
-                                                                  PassDigits pd, uint32_t* hist) {
+                                                                  PassDigits pd, uint32_t bins, uint32_t* hist) {
     __shared__ uint32_t s_hist[kMaxSortPasses * kRadixBins];
-    for (int i = threadIdx.x; i < pd.passes * kRadixBins; i += kThreads) s_hist[i] = 0;
+    for (int i = threadIdx.x; i < pd.passes * bins; i += kThreads) s_hist[i] = 0;
     __syncthreads();
     const uint32_t lane = lane_id();
     for (uint32_t base = blockIdx.x * kThreads + (threadIdx.x & ~31u); base < n; base += gridDim.x * kThreads) {
@@ -253,10 +257,10 @@ __global__ __launch_bounds__(kThreads) void sort_histogram_kernel(const K* __res
         const bool valid = i < n;
         K key = valid ? keys[i] : 0;
 #pragma unroll 1
-        for (int p = 0; p < pd.passes; ++p) hist_add(s_hist + p * kRadixBins, (uint32_t)(key >> pd.shift[p]) & pd.mask[p], valid);
+        for (int p = 0; p < pd.passes; ++p) hist_add(s_hist + p * bins, (uint32_t)(key >> pd.shift[p]) & pd.mask[p], valid);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < pd.passes * kRadixBins; i += kThreads)
+    for (int i = threadIdx.x; i < pd.passes * bins; i += kThreads)
         if (s_hist[i]) atomicAdd(hist + i, s_hist[i]);
 }
 
@@ -531,7 +535,10 @@ cudaError_t launch_morton(const Node2* nodes, uint32_t n, Control* ctrl, int key
         else
             morton_kernel<uint32_t, false><<<grid, kThreads, 0, s>>>(nodes, n, ctrl, (uint32_t*)keys, a);
     } else {
-        if (f.plan && a.pd.passes == 8)
+        if (f.plan && a.pd.passes == 4 && a.pd.mask[0] == (1u << kMaxRadixBits) - 1u)
+            morton_kernel<uint64_t, true, 4, 1 << kMaxRadixBits><<<grid, kThreads, 0, s>>>(nodes, n, ctrl,
+                                                                                           (uint64_t*)keys, a);
+        else if (f.plan && a.pd.passes == 8)
             morton_kernel<uint64_t, true, 8><<<grid, kThreads, 0, s>>>(nodes, n, ctrl, (uint64_t*)keys, a);
         else if (f.plan)
             morton_kernel<uint64_t, true><<<grid, kThreads, 0, s>>>(nodes, n, ctrl, (uint64_t*)keys, a);
@@ -554,11 +561,15 @@ cudaError_t launch_morton_scene(const Node2* nodes, uint32_t n, const nxb_aabb* 
 cudaError_t launch_sort_histogram(uint32_t key_bytes, const void* keys, uint32_t n, const SortPlan& plan,
                                   uint32_t* hist, cudaStream_t s) {
     PassDigits pd = to_digits(plan);
+    uint32_t widest = 1;
+    for (int p = 0; p < plan.passes; ++p) widest = std::max(widest, plan.bits[p]);
+    const uint32_t bins = 1u << std::max<uint32_t>(widest, kRadixBits);
+    if ((size_t)plan.passes * bins > (size_t)kMaxSortPasses * kRadixBins) return cudaErrorInvalidValue;
     uint32_t grid = grid_for(n, 4);
     if (key_bytes == 4)
-        sort_histogram_kernel<uint32_t><<<grid, kThreads, 0, s>>>((const uint32_t*)keys, n, pd, hist);
+        sort_histogram_kernel<uint32_t><<<grid, kThreads, 0, s>>>((const uint32_t*)keys, n, pd, bins, hist);
     else
-        sort_histogram_kernel<uint64_t><<<grid, kThreads, 0, s>>>((const uint64_t*)keys, n, pd, hist);
+        sort_histogram_kernel<uint64_t><<<grid, kThreads, 0, s>>>((const uint64_t*)keys, n, pd, bins, hist);
     return cudaGetLastError();
 }
 
