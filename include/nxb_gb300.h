@@ -278,8 +278,15 @@ nxb_status nxb_stage_radix_sort(uint32_t key_bytes, const void* d_keys_in, void*
  * cudaFree or allocating library call).
  *   - count may be at most NXB_NOALLOC_SORT_MAX_COUNT; larger counts return
  *     NXB_ERR_UNSUPPORTED (use nxb_stage_radix_sort for those).
- *   - The first call on a device looks up the array's device address with
- *     that device current; make that first call before any stream capture.
+ *   - The first call on a device is not yet allocation-free: with CUDA's
+ *     lazy module loading (the default) it loads the library's kernels on
+ *     that device, which creates the array and may synchronise, and it looks
+ *     up the array's device address with that device current.  Make that
+ *     first call once at start-up, outside the frame loop and before any
+ *     stream capture; later calls on that device allocate nothing.
+ *   - The address is kept per device for the life of the process: after
+ *     cudaDeviceReset the array may move, so do not use this entry point in
+ *     a process that resets a device it has already used.
  *   - Every call, from any thread or stream, shares the one array: calls
  *     whose work overlaps on the GPU race and corrupt each other's results.
  *     Order them on one stream (or wait on the previous call's work). */

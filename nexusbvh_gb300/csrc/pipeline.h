@@ -5,6 +5,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <mutex>
 
 #include "../../include/nxb_gb300.h"
 #include "common.cuh"
@@ -70,6 +71,22 @@ struct SortFallback {
     uint32_t* ticket;            // zero on entry
     uint32_t* done;              // plan.passes + 2 words, zero on entry
 };
+
+// Runs `set` (kernel attribute calls) once per device, with that device
+// current, from any number of host threads; later calls return its result.
+// Each call site passes its own lambda type and so has its own flags.
+template <typename F>
+cudaError_t once_per_device(F set) {
+    constexpr int kMaxDev = 64;
+    static std::once_flag once[kMaxDev];
+    static cudaError_t result[kMaxDev];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
+    std::call_once(once[dev], [&] { result[dev] = set(); });
+    return result[dev];
+}
 
 struct DeviceInfo {
     int sms;

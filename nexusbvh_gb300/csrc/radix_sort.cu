@@ -311,22 +311,6 @@ __global__ __launch_bounds__(kThreads, 4) void onesweep_kernel(const K* __restri
                                       s_local, s_tmp);
 }
 
-// Runs `set` (kernel attribute calls) once per device, with that device
-// current, from any number of host threads; later calls return its result.
-// Each call site passes its own lambda type and so has its own flags.
-template <typename F>
-cudaError_t once_per_device(F set) {
-    constexpr int kMaxDev = 64;
-    static std::once_flag once[kMaxDev];
-    static cudaError_t result[kMaxDev];
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
-    std::call_once(once[dev], [&] { result[dev] = set(); });
-    return result[dev];
-}
-
 // Dynamic shared memory above the 48 KB default (the 9-bit tables) and the
 // carveout for four tiles per SM: shared memory, not L1.
 template <typename Kern>
@@ -377,156 +361,163 @@ cudaError_t launch_pass_t(const K* kin, K* kout, const uint32_t* vin, uint32_t* 
 // in which equal keys are still in input order gives the same permutation).
 constexpr uint32_t kBucketWindow = 2048;  // buckets owned by one CTA start in its window
 constexpr uint32_t kBucketCap = 1024;     // largest bucket sorted in shared memory
+constexpr uint32_t kBucketHalo = 32;      // positions past the window read with it
 constexpr uint32_t kBucketSlots = kBucketWindow + kBucketCap;
+constexpr uint32_t kBucketWords = kBucketSlots / 32;  // bucket-start bitmask
 constexpr int kBucketThreads = 256;
-constexpr int kBucketPer = kBucketSlots / kBucketThreads;
-static_assert(kBucketSlots % kBucketThreads == 0, "whole slots per thread");
-static_assert(kBucketSlots <= 0xFFFFu, "16-bit bucket bounds");
-constexpr size_t kBucketSmem = (size_t)kBucketSlots * (8 + 4 + 4 + 2 + 2);
+static_assert(kBucketWindow % kBucketThreads == 0 && kBucketSlots % 32 == 0, "whole rows and words");
+constexpr size_t kBucketSmem = (size_t)kBucketSlots * (8 + 4) + 4 * kBucketWords;
 
 // One CTA per window of kBucketWindow positions: it owns the buckets that
 // start in its window (the last one may run on past the window, into at
-// most kBucketCap more positions), sorts each of them by its rank and
-// writes the keys that move.  Other CTAs only read the top bits of keys
-// outside their own buckets, which a permutation inside a bucket does not
-// change, so the sort runs in place.
-__global__ __launch_bounds__(kBucketThreads) void bucket_sort_kernel(uint64_t* keys, uint32_t* vals, uint32_t n,
-                                                                     uint32_t top_shift, uint32_t begin_bit,
-                                                                     uint32_t* overflow) {
+// most kBucketCap more positions), ranks each key in its bucket and writes
+// the keys that move.  Bucket starts are one bit per position, from warp
+// ballots: a warp's lanes hold 32 consecutive positions.  Other CTAs only
+// read the top bits of keys outside their own buckets, which a permutation
+// inside a bucket does not change, so the sort runs in place.
+__global__ __launch_bounds__(kBucketThreads, 6) void bucket_sort_kernel(uint64_t* keys, uint32_t* vals, uint32_t n,
+                                                                        uint32_t top_shift, uint32_t begin_bit,
+                                                                        uint32_t* overflow) {
     extern __shared__ __align__(16) unsigned char smem[];
     uint64_t* s_key = reinterpret_cast<uint64_t*>(smem);
     uint32_t* s_val = reinterpret_cast<uint32_t*>(s_key + kBucketSlots);
-    uint32_t* s_cmp = s_val + kBucketSlots;
-    uint16_t* s_bs = reinterpret_cast<uint16_t*>(s_cmp + kBucketSlots);
-    uint16_t* s_be = s_bs + kBucketSlots;
+    uint32_t* s_start = s_val + kBucketSlots;
     __shared__ uint32_t s_first, s_len, s_open;
-    __shared__ int32_t s_wmax[kBucketThreads / 32];
-    __shared__ uint32_t s_wmin[kBucketThreads / 32];
 
-    const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
+    const uint32_t tid = threadIdx.x, lane = lane_id();
     const uint32_t w0 = blockIdx.x * kBucketWindow;
-    const uint32_t wn = min(kBucketWindow, n - w0);
-    const uint64_t cmp_mask = (1ull << (top_shift - begin_bit)) - 1ull;
+    const uint32_t rest = n - w0;
+    const uint32_t wn = min(kBucketWindow, rest);
+    const uint32_t avail = min(rest, kBucketWindow + kBucketHalo);  // positions read in the first sweep
+    const uint32_t cmp_mask = (uint32_t)((1ull << (top_shift - begin_bit)) - 1ull);
     if (tid == 0) {
         s_first = kInvalid;
-        s_len = wn;
         s_open = 0;
     }
-    for (uint32_t j = tid; j < wn; j += kBucketThreads) {
-        const uint64_t k = __ldcg(keys + w0 + j);
-        s_key[j] = k;
-        s_val[j] = __ldcg(vals + w0 + j);
-        s_cmp[j] = (uint32_t)((k >> begin_bit) & cmp_mask);
-    }
+    for (uint32_t w = tid; w < kBucketWords; w += kBucketThreads) s_start[w] = 0;
     __syncthreads();
-    // the first bucket start of the window
-    for (uint32_t j = tid; j < wn; j += kBucketThreads) {
-        const bool start = j == 0 ? (w0 == 0 || (__ldcg(keys + w0 - 1) >> top_shift) != (s_key[0] >> top_shift))
-                                  : (s_key[j] >> top_shift) != (s_key[j - 1] >> top_shift);
-        if (start) {
-            atomicMin(&s_first, j);
-            break;  // a thread's later positions are larger
+    // ---- keys and values of positions [0, avail), every load issued
+    // before any is used, then the bucket-start bits
+    constexpr int kRows = (kBucketWindow + kBucketHalo + kBucketThreads - 1) / kBucketThreads;
+    {
+        uint64_t k[kRows];
+        uint32_t v[kRows];
+#pragma unroll
+        for (int r = 0; r < kRows; ++r) {
+            const uint32_t j = r * kBucketThreads + tid;
+            if (j < avail) {
+                k[r] = __ldcg(keys + w0 + j);
+                v[r] = __ldcg(vals + w0 + j);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < kRows; ++r) {
+            const uint32_t j = r * kBucketThreads + tid;
+            if (j < avail) {
+                s_key[j] = k[r];
+                s_val[j] = v[r];
+            }
         }
     }
+    const uint64_t before = tid == 0 && w0 > 0 ? __ldcg(keys + w0 - 1) >> top_shift : 0;
     __syncthreads();
-    const uint32_t s0 = s_first;
-    if (s0 == kInvalid) return;  // the window lies inside a bucket that started earlier
-    // the rest of the window's last bucket, past the window (warp 0)
-    if (warp == 0 && w0 + wn < n) {
-        const uint64_t last = s_key[wn - 1] >> top_shift;
-        uint32_t len = wn;
-        for (;;) {
-            const uint32_t g = w0 + len + lane;
-            const bool in = g < n && len + lane < kBucketSlots;
-            uint64_t k = 0;
-            if (in) k = __ldcg(keys + g);
-            const uint32_t stop = __ballot_sync(kFullMask, !in || (k >> top_shift) != last);
-            const uint32_t take = stop ? (uint32_t)(__ffs(stop) - 1) : 32u;
-            if (lane < take) {
-                s_key[len + lane] = k;
-                s_val[len + lane] = __ldcg(vals + g);
-                s_cmp[len + lane] = (uint32_t)((k >> begin_bit) & cmp_mask);
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) {
+        const uint32_t j = r * kBucketThreads + tid;
+        bool start = false;
+        if (j < avail) {
+            const uint64_t top = s_key[j] >> top_shift;
+            start = j == 0 ? w0 == 0 || before != top : (s_key[j - 1] >> top_shift) != top;
+        }
+        const uint32_t bits = __ballot_sync(kFullMask, start);
+        if (lane == 0) s_start[j >> 5] = bits;
+    }
+    __syncthreads();
+    // ---- the first bucket start of the window
+    if (tid < kBucketWindow / 32) {
+        const uint32_t b = s_start[tid];
+        if (b) atomicMin(&s_first, tid * 32 + __ffs(b) - 1);
+    }
+    // ---- the end of the window's last bucket: the first start past the
+    // window, searched further than the first sweep when it is not there
+    if (tid < 32) {
+        uint32_t len = rest;  // no start after the window: the last bucket ends with the keys
+        if (wn == kBucketWindow && rest > kBucketWindow) {
+            uint32_t found = kInvalid;
+            for (uint32_t w = kBucketWindow / 32 + lane; w * 32 < avail; w += 32) {
+                const uint32_t b = s_start[w];
+                if (b) found = min(found, w * 32 + __ffs(b) - 1);
             }
-            len += take;
-            if (!stop) continue;
-            // stopped at a new bucket, at the end of the keys, or with the
-            // slots full inside the bucket
-            if (len >= kBucketSlots && w0 + len < n && lane == 0 && (__ldcg(keys + w0 + len) >> top_shift) == last)
-                s_open = 1;
-            break;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) found = min(found, __shfl_xor_sync(kFullMask, found, o));
+            if (found != kInvalid) {
+                len = found;
+            } else if (avail < rest) {
+                // the last bucket runs past the first sweep: read on, 32 keys
+                // at a time, until its end, the end of the keys or the slots
+                const uint64_t last = s_key[avail - 1] >> top_shift;
+                uint32_t at = avail;
+                for (;;) {
+                    const uint32_t j = at + lane;
+                    const bool in = j < rest && j < kBucketSlots;
+                    uint64_t k = 0;
+                    if (in) k = __ldcg(keys + w0 + j);
+                    const uint32_t stop = __ballot_sync(kFullMask, !in || (k >> top_shift) != last);
+                    const uint32_t take = stop ? (uint32_t)(__ffs(stop) - 1) : 32u;
+                    if (lane < take) {
+                        s_key[j] = k;
+                        s_val[j] = __ldcg(vals + w0 + j);
+                    }
+                    at += take;
+                    if (stop) break;
+                }
+                len = at;
+                if (at >= kBucketSlots && at < rest && lane == 0 && (__ldcg(keys + w0 + at) >> top_shift) == last)
+                    s_open = 1;
+            } else {
+                len = avail;
+            }
         }
         if (lane == 0) s_len = len;
     }
     __syncthreads();
-    const uint32_t len = s_len;
-    if (s_open) {  // the last bucket is larger than the slots: leave everything to the fallback
+    const uint32_t s0 = s_first, len = s_len;
+    if (s0 == kInvalid) return;  // the window lies inside a bucket that started earlier
+    if (s_open) {                // its last bucket is larger than the slots: the fallback sorts everything
         if (tid == 0) atomicOr(overflow, 1u);
         return;
     }
-    // bucket bounds: bs = the last start <= j, be = the first start > j
-    // (or len), by a forward max-scan and a backward min-scan over blocked
-    // ranges of kBucketPer positions per thread
-    const uint32_t j0 = tid * kBucketPer;
-    auto is_start = [&](uint32_t j) -> bool {
-        return j == 0 ? s0 == 0 : (s_key[j] >> top_shift) != (s_key[j - 1] >> top_shift);
-    };
-    int32_t lbs[kBucketPer];
-    uint32_t lbe[kBucketPer];
-    int32_t cur = -1;
-#pragma unroll
-    for (int k = 0; k < kBucketPer; ++k) {
-        const uint32_t j = j0 + k;
-        if (j < len && is_start(j)) cur = (int32_t)j;
-        lbs[k] = cur;
-    }
-    uint32_t nxt = len;
-#pragma unroll
-    for (int k = kBucketPer - 1; k >= 0; --k) {
-        const uint32_t j = j0 + k;
-        lbe[k] = nxt;
-        if (j < len && is_start(j)) nxt = j;
-    }
-    // exclusive max-scan of cur over the threads before, min-scan of nxt over the threads after
-    int32_t incl_max = cur;
-    uint32_t incl_min = nxt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int32_t y = __shfl_up_sync(kFullMask, incl_max, o);
-        if (lane >= (uint32_t)o) incl_max = max(incl_max, y);
-        const uint32_t z = __shfl_down_sync(kFullMask, incl_min, o);
-        if (lane + o < 32u) incl_min = min(incl_min, z);
-    }
-    if (lane == 31) s_wmax[warp] = incl_max;
-    if (lane == 0) s_wmin[warp] = incl_min;
-    __syncthreads();
-    int32_t before = __shfl_up_sync(kFullMask, incl_max, 1);
-    if (lane == 0) before = -1;
-    uint32_t after = __shfl_down_sync(kFullMask, incl_min, 1);
-    if (lane == 31) after = len;
-    for (uint32_t w = 0; w < warp; ++w) before = max(before, s_wmax[w]);
-    for (uint32_t w = warp + 1; w < kBucketThreads / 32; ++w) after = min(after, s_wmin[w]);
-#pragma unroll
-    for (int k = 0; k < kBucketPer; ++k) {
-        const uint32_t j = j0 + k;
-        if (j < len) {
-            s_bs[j] = (uint16_t)max(lbs[k] >= 0 ? lbs[k] : before, 0);
-            s_be[j] = (uint16_t)(lbe[k] < len ? lbe[k] : after);
-        }
-    }
-    __syncthreads();
-    // rank of each key in its bucket: keys below it, and equal keys before it
+    // ---- rank of each key in its bucket: keys below it, and equal keys before it
+    const uint32_t* s_lo = reinterpret_cast<const uint32_t*>(s_key);  // low words of the keys
+    const uint32_t last_word = (len - 1) >> 5;
     bool over = false;
     for (uint32_t j = s0 + tid; j < len; j += kBucketThreads) {
-        const uint32_t bs = s_bs[j], be = s_be[j];
+        uint32_t w = j >> 5;
+        const uint32_t word = s_start[w];
+        // a bucket of one key (a start followed by a start): nothing moves
+        if ((word >> (j & 31)) & 1u) {
+            const uint32_t nxt = j + 1;
+            if (nxt >= len || ((nxt & 31) ? (word >> (nxt & 31)) & 1u : s_start[w + 1] & 1u)) continue;
+        }
+        // bucket bounds from the start bits: bs = the last start <= j,
+        // be = the first start > j (or len)
+        const uint32_t upto = 0xFFFFFFFFu >> (31 - (j & 31));  // bits <= j within the word
+        uint32_t m = word & upto;
+        while (m == 0) m = s_start[--w];  // s0 <= j is a start: the walk ends
+        const uint32_t bs = w * 32 + 31 - __clz(m);
+        w = j >> 5;
+        m = s_start[w] & ~upto;
+        while (m == 0 && w < last_word) m = s_start[++w];
+        const uint32_t be = m ? min(w * 32 + __ffs(m) - 1, len) : len;
         if (be - bs > kBucketCap) {
             over = true;
             continue;
         }
         if (be - bs == 1) continue;
-        const uint32_t c = s_cmp[j];
+        const uint32_t c = (s_lo[2 * j] >> begin_bit) & cmp_mask;
         uint32_t r = 0;
         for (uint32_t i = bs; i < be; ++i) {
-            const uint32_t ci = s_cmp[i];
+            const uint32_t ci = (s_lo[2 * i] >> begin_bit) & cmp_mask;
             r += (ci < c || (ci == c && i < j)) ? 1u : 0u;
         }
         const uint32_t dst = bs + r;
@@ -719,10 +710,7 @@ cudaError_t launch_sort63_hybrid(const uint64_t* keys_in, const uint32_t* vals_i
         if (e != cudaSuccess) return e;
     }
     {
-        cudaError_t attr = once_per_device([] {
-            return cudaFuncSetAttribute(bucket_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)kBucketSmem);
-        });
+        cudaError_t attr = once_per_device([] { return set_smem_attributes(bucket_sort_kernel, kBucketSmem); });
         if (attr != cudaSuccess) return attr;
         const uint32_t windows = (n + kBucketWindow - 1) / kBucketWindow;
         bucket_sort_kernel<<<windows, kBucketThreads, kBucketSmem, s>>>(keys_a, vals_a, n, kHybridTopShift, 1,
@@ -788,7 +776,9 @@ std::mutex g_noalloc_mu;
 unsigned char* g_noalloc_ptr[kNoAllocMaxDevices] = {};
 
 // Device address of the scratch on the current device, looked up once per
-// device (with that device current) on its first call.
+// device (with that device current) on its first call and kept for the
+// life of the process (a cudaDeviceReset would invalidate it; the header
+// tells callers not to reset a device they used this entry point on).
 cudaError_t noalloc_scratch(unsigned char** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

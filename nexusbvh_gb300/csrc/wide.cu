@@ -533,12 +533,10 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
 
 template <typename Seg, bool AUCTION>
 cudaError_t configure_smem() {
-    static bool configured = false;
-    if (configured) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(bvh8_kernel<Seg, AUCTION>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kSlotSmem);
-    if (!e) configured = true;
-    return e;
+    return once_per_device([] {
+        return cudaFuncSetAttribute(bvh8_kernel<Seg, AUCTION>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kSlotSmem);
+    });
 }
 
 template <typename Seg, bool AUCTION>

@@ -123,4 +123,6 @@ def by_name(name: str) -> np.ndarray:
         return clustered()
     if name == "clustered4m":
         return clustered(4_194_304)
+    if name == "clustered28m":  # the served workload's injected build
+        return clustered(28_311_552, seed=5)
     raise KeyError(name)

@@ -6,7 +6,8 @@ ships inside the CUDA toolkit (CCCL 3.0.1 with CUDA 13.0).  Its CMake build
 is not used: this script compiles the sources directly.
 
   stage():  copies the reference's source files verbatim from the read-only
-            checkout (default /root/reference, or $NXB_REFERENCE) into
+            checkout ($NXB_REFERENCE, else a `reference` directory beside
+            this repository's checkout) into
             oracle/_ref/src/, plus one patched copy of BinaryBuilder.cu whose
             SEARCH_RADIUS can be set with -D (the reference hard-codes 8).
             oracle/_ref/ is git-ignored: nothing of the reference is
@@ -45,7 +46,10 @@ ARCH = ["-gencode", "arch=compute_103,code=sm_103"]
 
 
 def reference_root() -> Path:
-    return Path(os.environ.get("NXB_REFERENCE", "/root/reference"))
+    env = os.environ.get("NXB_REFERENCE")
+    if env:
+        return Path(env)
+    return ORACLE_DIR.parent.parent / "reference"  # a checkout beside this repository's
 
 
 def lib_path(radius: int = 8) -> Path:

@@ -694,100 +694,10 @@ Node8 make_node8(const Box& bounds, const uint32_t* child, uint32_t child_base, 
     return nd;
 }
 
-// BuildBVH8Kernel (WideConverter.cu:225-414), with the work slots processed
-// in increasing order (every slot is written by a parent in a lower slot).
-int bvh8(const Node2* nodes, uint32_t n, uint32_t root, Node8* out, uint32_t cap, uint32_t* prim_idx,
-         uint32_t* node_count, uint32_t* leaf_count, bool use_auction = false) {
-    if (n == 1) {  // CreateBVH8SingleLeaf (WideConverter.cu:209-222)
-        uint32_t child[8] = {0};
-        out[0] = make_node8(nodes[0].b, child, 0, 0, 0xFFFFFFF0u, 0, 1, nodes);
-        prim_idx[0] = 0;
-        *node_count = 1;
-        *leaf_count = 1;
-        return 0;
-    }
-    std::vector<uint64_t> pairs(n, ~0ull);
-    pairs[0] = (uint64_t)root << 32;
-    uint32_t node_ctr = 1, leaf_ctr = 0, work_alloc = 1;
-    int err = 0;
-    for (uint32_t w = 0; w < n; ++w) {
-        while (true) {
-            uint64_t pr = pairs[w];
-            uint32_t b2 = (uint32_t)(pr >> 32), b8 = (uint32_t)pr;
-            if (b2 == kInvalid) return err | 1;
-            const Node2& nd = nodes[b2];
-            if (nd.left == kInvalid) {
-                if (b8 >= n) return err | 2;
-                prim_idx[b8] = nd.right;
-                break;
-            }
-            uint32_t inner = 0, count = 0, child[8];
-            uint32_t lr[2] = {nd.left, nd.right};
-            int msb = 0;
-            while (true) {
-                float a0 = area(nodes[lr[0]].b), a1 = area(nodes[lr[1]].b);
-                uint32_t first = a0 < a1 ? 0 : 1;
-                for (uint32_t i = 0; i < 2; ++i) {
-                    uint32_t idx = i == 0 ? (uint32_t)msb : count;
-                    if (nodes[lr[first]].left != kInvalid) inner |= 1u << idx;
-                    child[idx] = lr[first];
-                    count++;
-                    first = !first;
-                }
-                msb = inner ? 31 - __builtin_clz(inner) : -1;
-                if (msb < 0 || count == 8) break;
-                inner &= ~(1u << msb);
-                count--;
-                uint32_t ni = child[msb];
-                lr[0] = nodes[ni].left;
-                lr[1] = nodes[ni].right;
-            }
-            float pc[3];
-            for (int a = 0; a < 3; ++a) pc[a] = fadd(nd.b.mn[a], nd.b.mx[a]);
-            uint32_t asg = 0;
-            if (!use_auction || !auction(nd.b, child, count, nodes, &asg)) asg = greedy(pc, child, count, nodes);
-            uint32_t new_inner = 0, leaf = 0;
-            for (uint32_t i = 0; i < 8; ++i) {
-                if (nib(asg, i) == 0xF) continue;
-                uint32_t bit = (inner >> nib(asg, i)) & 1u;
-                new_inner |= bit << i;
-                leaf |= (bit ^ 1u) << i;
-            }
-            inner = new_inner;
-            uint32_t inner_count = (uint32_t)__builtin_popcount(inner);
-            uint32_t lc = count - inner_count;
-            uint32_t child_base = node_ctr;
-            node_ctr += inner_count;
-            uint32_t work_base = work_alloc;
-            work_alloc += count - 1;
-            uint32_t prim_base = 0;
-            if (lc > 0) {
-                prim_base = leaf_ctr;
-                leaf_ctr += lc;
-            }
-            if (node_ctr > cap || work_alloc > n) return err | 4;
-            for (uint32_t i = 0; i < 8; ++i) {
-                if (nib(asg, i) == 0xF) continue;
-                uint64_t pr2 = (uint64_t)child[nib(asg, i)] << 32;
-                if (inner & (1u << i))
-                    pr2 |= child_base + below(inner, i);
-                else
-                    pr2 |= prim_base + below(leaf, i);
-                uint32_t c = below(inner | leaf, i);
-                uint32_t idx = c == 0 ? w : work_base + c - 1;
-                pairs[idx] = pr2;
-            }
-            out[b8] = make_node8(nd.b, child, child_base, prim_base, asg, inner, leaf, nodes);
-        }
-    }
-    *node_count = node_ctr;
-    *leaf_count = leaf_ctr;
-    return err;
-}
-
-// One BVH8 node of bvh8_levels before it is numbered: its children (BVH2
-// indices), slot assignment and inner / leaf slot masks, exactly as one work
-// item of bvh8() computes them.
+// One BVH8 node before it is numbered: its children (BVH2 indices), slot
+// assignment and inner / leaf slot masks.  This is one work item of
+// BuildBVH8Kernel (WideConverter.cu:284-330 the expansion, :332-362 the slot
+// assignment); bvh8() and bvh8_levels() both collapse through it.
 struct CollapsedNode {
     uint32_t child[8];
     uint32_t asg, inner, leaf;
@@ -828,6 +738,69 @@ void collapse_node(const Node2* nodes, uint32_t b2, bool use_auction, CollapsedN
         c.inner |= bit << i;
         c.leaf |= (bit ^ 1u) << i;
     }
+}
+
+// BuildBVH8Kernel (WideConverter.cu:225-414), with the work slots processed
+// in increasing order (every slot is written by a parent in a lower slot).
+int bvh8(const Node2* nodes, uint32_t n, uint32_t root, Node8* out, uint32_t cap, uint32_t* prim_idx,
+         uint32_t* node_count, uint32_t* leaf_count, bool use_auction = false) {
+    if (n == 1) {  // CreateBVH8SingleLeaf (WideConverter.cu:209-222)
+        uint32_t child[8] = {0};
+        out[0] = make_node8(nodes[0].b, child, 0, 0, 0xFFFFFFF0u, 0, 1, nodes);
+        prim_idx[0] = 0;
+        *node_count = 1;
+        *leaf_count = 1;
+        return 0;
+    }
+    std::vector<uint64_t> pairs(n, ~0ull);
+    pairs[0] = (uint64_t)root << 32;
+    uint32_t node_ctr = 1, leaf_ctr = 0, work_alloc = 1;
+    int err = 0;
+    for (uint32_t w = 0; w < n; ++w) {
+        while (true) {
+            uint64_t pr = pairs[w];
+            uint32_t b2 = (uint32_t)(pr >> 32), b8 = (uint32_t)pr;
+            if (b2 == kInvalid) return err | 1;
+            const Node2& nd = nodes[b2];
+            if (nd.left == kInvalid) {
+                if (b8 >= n) return err | 2;
+                prim_idx[b8] = nd.right;
+                break;
+            }
+            CollapsedNode cn;
+            collapse_node(nodes, b2, use_auction, cn);
+            const uint32_t* child = cn.child;
+            const uint32_t asg = cn.asg, inner = cn.inner, leaf = cn.leaf;
+            const uint32_t count = (uint32_t)__builtin_popcount(inner | leaf);
+            uint32_t inner_count = (uint32_t)__builtin_popcount(inner);
+            uint32_t lc = count - inner_count;
+            uint32_t child_base = node_ctr;
+            node_ctr += inner_count;
+            uint32_t work_base = work_alloc;
+            work_alloc += count - 1;
+            uint32_t prim_base = 0;
+            if (lc > 0) {
+                prim_base = leaf_ctr;
+                leaf_ctr += lc;
+            }
+            if (node_ctr > cap || work_alloc > n) return err | 4;
+            for (uint32_t i = 0; i < 8; ++i) {
+                if (nib(asg, i) == 0xF) continue;
+                uint64_t pr2 = (uint64_t)child[nib(asg, i)] << 32;
+                if (inner & (1u << i))
+                    pr2 |= child_base + below(inner, i);
+                else
+                    pr2 |= prim_base + below(leaf, i);
+                uint32_t c = below(inner | leaf, i);
+                uint32_t idx = c == 0 ? w : work_base + c - 1;
+                pairs[idx] = pr2;
+            }
+            out[b8] = make_node8(nd.b, child, child_base, prim_base, asg, inner, leaf, nodes);
+        }
+    }
+    *node_count = node_ctr;
+    *leaf_count = leaf_ctr;
+    return err;
 }
 
 // The same collapse level by level, for the timed CPU baseline: the nodes of

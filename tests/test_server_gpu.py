@@ -100,6 +100,37 @@ def test_server_same_tree_alone_and_mixed(gpu, orc):
     srv.close()
 
 
+def test_server_mixed_batch_matches_oracle(gpu, orc):
+    """Requests that the server builds together in one batched launch each
+    equal the oracle's tree for that mesh alone: the oracle's H-PLOC and
+    BVH8 collapse (oracle/nxb_oracle.cpp) over the mesh's own GPU Morton
+    order, which run_chain checks stage by stage."""
+    from tests.test_gpu_parity import run_chain
+    srv = nxb.Server(streams=1)
+    t_big = srv.submit(scenes.clustered(1_500_000, seed=6), nxb.BuildConfig(prioritize_speed=True))
+    meshes = [scenes.uniform_soup(700 + 311 * i, seed=60 + i) if i % 3 == 0 else
+              scenes.clustered(500 + 173 * i, seed=70 + i, components=6) if i % 3 == 1 else
+              scenes.batch_meshes([900 + 97 * i], seed=80 + i) for i in range(9)]
+    tickets = [srv.submit(m if i % 2 else S.dev(m), nxb.BuildConfig(prioritize_speed=True))
+               for i, m in enumerate(meshes)]
+    srv.wait(t_big)
+    srv.release(t_big)
+    checked = 0
+    for t, m in zip(tickets, meshes):
+        r = srv.wait(t)
+        assert r.status == 0
+        n = m.shape[0]
+        b8, prim = nxb.Server.bvh8_host(r)
+        chain = run_chain(m, 30, orc)
+        b8_o, prim_o, err = orc.bvh8(chain["b2"], n, 2 * n - 2)
+        assert err == 0
+        assert orc.compare_bvh8(b8, prim, b8_o, prim_o, n) == 0
+        checked += r.batched_with > 1
+        srv.release(t)
+    assert checked >= 2, "the small requests were expected to be built together"
+    srv.close()
+
+
 def test_server_admission_and_budget(gpu, orc):
     budget = 96 << 20
     srv = nxb.Server(budget_bytes=budget, streams=4, batch_max_prims=1)  # no batching: plain builds only

@@ -67,3 +67,33 @@ def test_noalloc_sort_rejects_oversize(gpu):
     d = torch.zeros(n, dtype=torch.int32, device="cuda")
     o = torch.zeros(n, dtype=torch.int32, device="cuda")
     assert noalloc(gpu)(4, d.data_ptr(), o.data_ptr(), None, o.data_ptr(), n, 0, 32, None, None) == 2
+
+
+def test_noalloc_sort_allocates_nothing_once_warm(gpu):
+    """After a first (warm-up) call on the device, a call leaves the
+    device's free memory exactly as it was: no allocation happens."""
+    import torch
+
+    from tests import stages as S
+    n = 50_000
+    keys = np.random.default_rng(5).integers(0, 1 << 62, size=n, dtype=np.uint64)
+    d_keys = S.dev(keys.view(np.int64))
+    out_k = torch.empty_like(d_keys)
+    out_v = torch.empty(n, dtype=torch.int32, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    fn = noalloc(gpu)
+
+    def call():
+        status = fn(8, d_keys.data_ptr(), out_k.data_ptr(), None, out_v.data_ptr(), n, 1, 64, err.data_ptr(),
+                    S.stream())
+        torch.cuda.synchronize()
+        assert status == 0 and int(err.item()) == 0
+
+    call()  # warm-up: loads the kernels on this device, looks up the array
+    free_before = torch.cuda.mem_get_info()[0]
+    call()
+    call()
+    assert torch.cuda.mem_get_info()[0] == free_before
+    want = np.argsort(keys >> np.uint64(1), kind="stable").astype(np.uint32)
+    np.testing.assert_array_equal(S.host(out_v).view(np.uint32), want)
+
