@@ -295,6 +295,15 @@ def run_ours(args, world, rank, local):
         e2e_ov_s = float(t.item())
     e2e_ov_value = world * n * e2e_steps / e2e_ov_s / 1e6
 
+    # the batched and served forms, measured on the same GPU after the plain
+    # line (one GPU only: with several ranks each runs the plain replica)
+    forms = {}
+    if world == 1 and not args.no_forms:
+        del d_in, d_ins
+        torch.cuda.empty_cache()
+        forms["batched"] = batch_summary(measure_batch(args, 1, 0, local, steps=10, warmup=3, autotune=True,
+                                                       fusion_sweep=False, loop_baseline=True))
+        forms["served"] = served_summary(measure_served(args, 1, 0, local, requests=200, warmup=20, burst=1000))
     if rank != 0:
         return
     pk = peaks()
@@ -307,12 +316,22 @@ def run_ours(args, world, rank, local):
                         "frac": round(gbs / pk["hbm_gbs"], 3)}
     dominant = max(STAGES, key=lambda s: stage_ms[s])
     traffic = None
+    clk = clocks.summary()
     tp = ROOT / "profiles" / "dram_traffic.json"
-    if tp.exists():
-        tj = json.loads(tp.read_text())
-        key = f"{args.workload}/{key_bits}/{dominant}"
-        if key in tj:
-            traffic = int(tj[key]["bytes_per_tri"] * n)
+    counters = json.loads(tp.read_text()) if tp.exists() else {}
+    key = f"{args.workload}/{key_bits}/{dominant}"
+    if key in counters:
+        traffic = int(counters[key]["bytes_per_tri"] * n)
+    # issue side of the latency-bound kernels: warp instructions per launch
+    # (ncu count per triangle, scaled) against the SMs' issue slots
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    mhz = clk.get("sm_mhz") or 2070.0
+    for stg in ("hploc", "bvh8"):
+        c = counters.get(f"{args.workload}/{key_bits}/{stg}", {})
+        if "warp_inst_per_tri" in c:
+            inst = c["warp_inst_per_tri"] * n
+            per_stage[stg]["warp_inst"] = int(inst)
+            per_stage[stg]["issue_frac"] = round(inst / (stage_ms[stg] * 1e-3 * sms * 4 * mhz * 1e6), 3)
     line = {
         "metric": "Mtris/s full build (bounds, Morton, radix sort, H-PLOC BVH2, BVH8)",
         "value": round(value, 2),
@@ -340,6 +359,7 @@ def run_ours(args, world, rank, local):
             "e2e_overlapped_copy": {"value": round(e2e_ov_value, 2), "unit": "Mtris/s",
                                     "how": "the e2e calls with step k+1's host->device copy on a second stream "
                                            "overlapping step k's build (supplementary; e2e is the serial loop)"},
+            **forms,
         },
         "roofline": {
             "kernel": dominant,
@@ -350,21 +370,27 @@ def run_ours(args, world, rank, local):
             "frac": per_stage[dominant]["frac"],
             "traffic": traffic,
             "peak_source": pk["source"],
+            "issue_frac": per_stage[dominant].get("issue_frac"),
         },
         "e2e": {"value": round(e2e_value, 2), "unit": "Mtris/s", "h2d_bytes_per_step": 36 * n,
                 "d2h_bytes_per_step": ctypes.sizeof(nxb.CResult),
                 "call": "nxb_build_bvh8 (C ABI, allocates outputs) after a pinned host->device copy"},
-        "gpu_launches": (6 + passes) * args.steps,
-        "clocks": clocks.summary(),
+        # per build: bounds, Morton, the sort (30-bit: 4 passes; 63-bit: 4
+        # passes, the bucket sort and the fallback launch), H-PLOC, BVH8
+        # queue init, BVH8, finalize
+        "gpu_launches": (6 + (4 if key_bits == 30 else 6)) * args.steps,
+        "clocks": clk,
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(prims_np, key_bits, args.radius, args.cpu_sample)
     print(json.dumps(line), flush=True)
 
 
-def run_batch(args, world, rank, local):
-    """Batched form: all meshes in one graph-replayed pipeline (nxb_batch_*),
-    next to a loop of plain builds over the same meshes."""
+def measure_batch(args, world, rank, local, steps: int, warmup: int, autotune: bool, fusion_sweep: bool,
+                  loop_baseline: bool, cpu_baseline_tris: int = 0) -> dict:
+    """The batched form on the batch1024 meshes: all meshes in one
+    graph-replayed pipeline (nxb_batch_*), next to a loop of plain builds over
+    the same meshes.  Returns the measurements (rank 0's line fields)."""
     import torch
     import nexusbvh_gb300 as nxb
     from nexusbvh_gb300 import scenes
@@ -373,7 +399,7 @@ def run_batch(args, world, rank, local):
 
     torch.cuda.set_device(local)
     lib = nxb.load()
-    meshes_all, seed = BATCH_WORKLOADS[args.workload]
+    meshes_all, seed = BATCH_WORKLOADS["batch1024"]
     counts_all = scenes.batch_counts(meshes_all, seed=seed)
     prims_all = scenes.batch_meshes(counts_all, seed=seed)
     n_all = prims_all.shape[0]
@@ -391,7 +417,7 @@ def run_batch(args, world, rank, local):
     sptr = int(stream.cuda_stream)
     batch = nxb.Batch(counts, config=nxb.BuildConfig(prioritize_speed=True, search_radius=args.radius))
     t_tune = time.perf_counter()
-    tuning = batch.tuning() if args.no_autotune else batch.autotune(d_prims, repeats=2)
+    tuning = batch.autotune(d_prims, repeats=2) if autotune else batch.tuning()
     t_tune = time.perf_counter() - t_tune
 
     def timed_build(groups: int, reps: int = 5) -> float:
@@ -411,10 +437,9 @@ def run_batch(args, world, rank, local):
         return statistics.median(ms)
 
     chosen = batch.tuning()
-    # the fusion-point sweep is part of the tuning report (skipped with --no-autotune)
-    fusion = None if args.no_autotune else {f"groups_{g}_ms": round(timed_build(g), 4) for g in (1, 2, 4, 8)}
+    fusion = {f"groups_{g}_ms": round(timed_build(g), 4) for g in (1, 2, 4, 8)} if fusion_sweep else None
     batch.set_tuning(chosen)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         batch.build_async(d_prims)
     batch.wait(results=False)
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -423,13 +448,13 @@ def run_batch(args, world, rank, local):
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         start.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             batch.build_async(d_prims)
         stop.record(stream)
         torch.cuda.synchronize()
     res = batch.wait(results=True)
     elapsed = start.elapsed_time(stop)
-    value = dist.whole_job_rate(n * args.steps, elapsed * 1e-3, device="cuda") / 1e6
+    value = dist.whole_job_rate(n * steps, elapsed * 1e-3, device="cuda") / 1e6
     elapsed = dist.max_over_ranks(elapsed, device="cuda")
     n8 = sum(r.bvh8_node_count for r in res)
 
@@ -438,7 +463,7 @@ def run_batch(args, world, rank, local):
     d_in = torch.empty_like(d_prims)
     d_in.copy_(h_prims, non_blocking=True)
     batch.build(d_in)  # capture for this buffer
-    e2e_steps = max(3, min(args.steps, 10))
+    e2e_steps = max(3, min(steps, 10))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -446,6 +471,7 @@ def run_batch(args, world, rank, local):
         batch.build(d_in)
     e2e_s = time.perf_counter() - t0
     e2e_value = dist.whole_job_rate(n * e2e_steps, e2e_s, device="cuda") / 1e6
+    del d_in, h_prims
 
     # the loop of plain builds the batch replaces: the reference-shaped call
     # per mesh (allocating, synchronising), and nxb_build_async per mesh into
@@ -464,27 +490,27 @@ def run_batch(args, world, rank, local):
                                          None), "nxb_build_bvh8")
             nxb.check(lib.nxb_free_device_bvh8(ctypes.byref(out)), "nxb_free_device_bvh8")
 
-    b = nxb.Builder()
-    big = int(max(counts))
-    sz = b.sizes(big, cfg)
-    ws = b.workspace(sz.workspace_bytes)
-    b2 = torch.empty((sz.bvh2_node_count, 32), dtype=torch.uint8, device="cuda")
-    b8 = torch.empty((sz.bvh8_node_capacity, 80), dtype=torch.uint8, device="cuda")
-    pidx = torch.empty(big, dtype=torch.int32, device="cuda")
-    rbuf = torch.zeros(64, dtype=torch.uint8, device="cuda")
-
-    def loop_async():
-        for m in range(meshes):
-            k = int(counts[m])
-            if k == 0:
-                continue
-            ptr = d_prims.data_ptr() + int(off[m]) * 36
-            nxb.check(lib.nxb_build_async(ptr, nxb.NXB_PRIM_TRIANGLE, k, ctypes.byref(c), ws.data_ptr(), ws.numel(),
-                                          b2.data_ptr(), b8.data_ptr(), pidx.data_ptr(), rbuf.data_ptr(), sptr),
-                      "nxb_build_async")
-
     t_loop = t_loop_async = float("nan")
-    if not args.no_loop_baseline:
+    if loop_baseline:
+        b = nxb.Builder()
+        big = int(max(counts))
+        sz = b.sizes(big, cfg)
+        ws = b.workspace(sz.workspace_bytes)
+        b2 = torch.empty((sz.bvh2_node_count, 32), dtype=torch.uint8, device="cuda")
+        b8 = torch.empty((sz.bvh8_node_capacity, 80), dtype=torch.uint8, device="cuda")
+        pidx = torch.empty(big, dtype=torch.int32, device="cuda")
+        rbuf = torch.zeros(64, dtype=torch.uint8, device="cuda")
+
+        def loop_async():
+            for m in range(meshes):
+                k = int(counts[m])
+                if k == 0:
+                    continue
+                ptr = d_prims.data_ptr() + int(off[m]) * 36
+                nxb.check(lib.nxb_build_async(ptr, nxb.NXB_PRIM_TRIANGLE, k, ctypes.byref(c), ws.data_ptr(),
+                                              ws.numel(), b2.data_ptr(), b8.data_ptr(), pidx.data_ptr(),
+                                              rbuf.data_ptr(), sptr), "nxb_build_async")
+
         loop_plain()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -498,56 +524,25 @@ def run_batch(args, world, rank, local):
         stop.record(stream)
         torch.cuda.synchronize()
         t_loop_async = start.elapsed_time(stop) / 1e3
-    if rank != 0:
-        return
-    pk = peaks()
+        del ws, b2, b8, pidx, rbuf
     passes = -(-(30 + max(1, (meshes - 1).bit_length())) // int(tuning.sort_digit_bits))
     per_tri = (algorithmic_bytes("scene_bounds", 8, passes, 0) + algorithmic_bytes("morton", 8, passes, 0)
                + 4.0 + algorithmic_bytes("radix_sort", 8, passes, 0) + algorithmic_bytes("hploc", 8, passes, 0)
                + algorithmic_bytes("bvh8", 8, passes, n8 / n))
-    ms = elapsed / args.steps
-    gbs = per_tri * n / (ms * 1e-3) / 1e9
-    line = {
-        "metric": "Mtris/s batched build (1024 meshes, bounds, Morton, radix sort, H-PLOC BVH2, BVH8)",
-        "value": round(value, 2), "unit": "Mtris/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (seeded generators standing in for the reference's scene files)",
-        "config": {
-            "workload": WORKLOADS[args.workload][0], "meshes": meshes_all, "n_tris": n_all,
-            "rank0_meshes": meshes, "rank0_tris": n, "key_bits": 30,
-            "search_radius": int(tuning.search_radius),
-            "parallelism": f"meshes sharded over {world} GPU(s) by size, no collective",
-            "l2": "inputs larger than L2 (1.3 GB of triangles), no flush needed",
-            "tuning": {"sort_digit_bits": int(tuning.sort_digit_bits), "sort_passes": passes,
-                       "hploc_ctas_per_sm": int(tuning.hploc_ctas_per_sm),
-                       "fusion_groups": int(tuning.fusion_groups), "block_size": int(tuning.block_size),
-                       "fusion_point": fusion,
-                       "candidates": int(tuning.candidates_tried), "tune_s": round(t_tune, 2)},
-            "bvh8_nodes": int(n8),
-            "loop_plain_api_ms": _num(t_loop * 1e3),
-            "loop_plain_api_mtris_s": _num(n / t_loop / 1e6),
-            "loop_async_ms": _num(t_loop_async * 1e3),
-            "speedup_vs_loop_plain_api": _num(t_loop * 1e3 / ms),
-            "speedup_vs_loop_async": _num(t_loop_async * 1e3 / ms),
-        },
-        "roofline": {"kernel": "whole batched pipeline", "bound": "hbm", "achieved": round(gbs, 1),
-                     "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(gbs / pk["hbm_gbs"], 3), "traffic": None,
-                     "peak_source": pk["source"]},
-        "e2e": {"value": round(e2e_value, 2), "unit": "Mtris/s", "h2d_bytes_per_step": 36 * n,
-                "d2h_bytes_per_step": 52 * meshes + 4,
-                "call": "nxb_batch_build (graph replay + wait + per-mesh results) after a pinned host->device copy"},
-        # per build: tile ranges, bounds, Morton, the sort passes, BVH8 queue
-        # init, H-PLOC, BVH8, finalize (one mesh group)
-        "gpu_launches": (7 + passes) * args.steps,
+    ms = elapsed / steps
+    out_d = {
+        "value": value, "ms": ms, "n": n, "n_all": n_all, "meshes": meshes, "meshes_all": meshes_all,
+        "tuning": tuning, "passes": passes, "fusion": fusion, "t_tune": t_tune, "n8": n8,
+        "gbs": per_tri * n / (ms * 1e-3) / 1e9, "e2e": e2e_value, "t_loop": t_loop, "t_loop_async": t_loop_async,
         "clocks": clocks.summary(),
     }
-    if not args.no_cpu_baseline:
+    if cpu_baseline_tris and rank == 0:
         import oracle
         oracle.set_level_collapse(True)
         t = time.perf_counter()
         done = 0
         m = 0
-        while done < args.cpu_sample and m < meshes:
+        while done < cpu_baseline_tris and m < meshes:
             k = int(counts[m])
             if k:
                 r = oracle.build(np.ascontiguousarray(prims_np[off[m]:off[m + 1]]), 30, args.radius)
@@ -555,9 +550,75 @@ def run_batch(args, world, rank, local):
                 done += k
             m += 1
         dt = time.perf_counter() - t
-        line["cpu_baseline"] = {"value": round(done / dt / 1e6, 3), "unit": "Mtris/s", "cores": oracle.threads(),
-                                "kind": "port", "sample": f"the first {m} meshes ({done:,} triangles), one CPU build "
-                                                          f"each, in {dt:.2f} s"}
+        out_d["cpu_baseline"] = {"value": round(done / dt / 1e6, 3), "unit": "Mtris/s", "cores": oracle.threads(),
+                                 "kind": "port", "sample": f"the first {m} meshes ({done:,} triangles), one CPU "
+                                                           f"build each, in {dt:.2f} s"}
+    del d_prims, batch
+    torch.cuda.empty_cache()
+    return out_d
+
+
+def batch_summary(b: dict) -> dict:
+    """The batched measurements as a compact record."""
+    t = b["tuning"]
+    return {
+        "mtris_s": round(b["value"], 2), "ms_per_build": round(b["ms"], 4), "meshes": b["meshes_all"],
+        "n_tris": b["n_all"],
+        "tuning": {"sort_digit_bits": int(t.sort_digit_bits), "sort_passes": b["passes"],
+                   "search_radius": int(t.search_radius), "hploc_ctas_per_sm": int(t.hploc_ctas_per_sm),
+                   "fusion_groups": int(t.fusion_groups), "block_size": int(t.block_size),
+                   "candidates": int(t.candidates_tried), "tune_s": round(b["t_tune"], 2)},
+        "loop_plain_api_ms": _num(b["t_loop"] * 1e3),
+        "loop_async_ms": _num(b["t_loop_async"] * 1e3),
+        "speedup_vs_loop_plain_api": _num(b["t_loop"] * 1e3 / b["ms"]),
+        "speedup_vs_loop_async": _num(b["t_loop_async"] * 1e3 / b["ms"]),
+        "target_speedup": 3.0,
+        "e2e_mtris_s": round(b["e2e"], 2),
+    }
+
+
+def run_batch(args, world, rank, local):
+    """Batched form: the batch1024 line."""
+    b = measure_batch(args, world, rank, local, args.steps, args.warmup, autotune=not args.no_autotune,
+                      fusion_sweep=not args.no_autotune, loop_baseline=not args.no_loop_baseline,
+                      cpu_baseline_tris=0 if args.no_cpu_baseline else args.cpu_sample)
+    if rank != 0:
+        return
+    pk = peaks()
+    tuning, meshes, n = b["tuning"], b["meshes"], b["n"]
+    line = {
+        "metric": "Mtris/s batched build (1024 meshes, bounds, Morton, radix sort, H-PLOC BVH2, BVH8)",
+        "value": round(b["value"], 2), "unit": "Mtris/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(b["ms"], 4), "higher_is_better": True, "scaling": "strong",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generators standing in for the reference's scene files)",
+        "config": {
+            "workload": WORKLOADS[args.workload][0], "meshes": b["meshes_all"], "n_tris": b["n_all"],
+            "rank0_meshes": meshes, "rank0_tris": n, "key_bits": 30,
+            "search_radius": int(tuning.search_radius),
+            "parallelism": f"meshes sharded over {world} GPU(s) by size, no collective",
+            "l2": "inputs larger than L2 (1.3 GB of triangles), no flush needed",
+            "tuning": dict(batch_summary(b)["tuning"], fusion_point=b["fusion"]),
+            "bvh8_nodes": int(b["n8"]),
+            "loop_plain_api_ms": _num(b["t_loop"] * 1e3),
+            "loop_plain_api_mtris_s": _num(n / b["t_loop"] / 1e6),
+            "loop_async_ms": _num(b["t_loop_async"] * 1e3),
+            "speedup_vs_loop_plain_api": _num(b["t_loop"] * 1e3 / b["ms"]),
+            "speedup_vs_loop_async": _num(b["t_loop_async"] * 1e3 / b["ms"]),
+        },
+        "roofline": {"kernel": "whole batched pipeline", "bound": "hbm", "achieved": round(b["gbs"], 1),
+                     "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(b["gbs"] / pk["hbm_gbs"], 3),
+                     "traffic": None, "peak_source": pk["source"]},
+        "e2e": {"value": round(b["e2e"], 2), "unit": "Mtris/s", "h2d_bytes_per_step": 36 * n,
+                "d2h_bytes_per_step": 52 * meshes + 4,
+                "call": "nxb_batch_build (graph replay + wait + per-mesh results) after a pinned host->device copy"},
+        # per build: tile ranges, bounds, Morton, the sort passes, BVH8 queue
+        # init, H-PLOC, BVH8, finalize (one mesh group)
+        "gpu_launches": (7 + b["passes"]) * args.steps,
+        "clocks": b["clocks"],
+    }
+    if "cpu_baseline" in b:
+        line["cpu_baseline"] = b["cpu_baseline"]
     print(json.dumps(line), flush=True)
 
 
@@ -577,131 +638,178 @@ def served_requests(count: int, seed: int = 11):
     return out
 
 
-def run_served(args, world, rank, local):
-    """Served form: a build server (nxb_server_*) fed Poisson arrivals; per
-    request latency = submit -> completion, p50/p99 over the timed requests."""
+def burst_requests(count: int, seed: int = 21):
+    """(kind, n, key_bits) of a burst of small requests: configuration-0 and
+    -1 style meshes (kind 0 soup, kind 1 sphere, alternating), n log-U[1024,
+    65536], 30-bit codes (the size and key width the server may batch)."""
+    rng = np.random.default_rng(seed)
+    return [(i % 2, int(np.exp(rng.uniform(np.log(1024), np.log(65536 + 1)))), 30) for i in range(count)]
+
+
+def _pctl(x, q):
+    return float(np.percentile(x, q)) if len(x) else float("nan")
+
+
+def measure_served(args, world, rank, local, requests: int, warmup: int, burst: int = 1000) -> dict:
+    """Served form: a build server (nxb_server_*) fed Poisson arrivals (200
+    requests/s, the configuration's stream) and a burst of small requests
+    that arrives faster than the GPU serves them; per request latency =
+    submit -> completion.  Each pass is compared with the same arrivals
+    served by serial plain builds."""
     import threading
+    import queue as _q
     import torch
     import nexusbvh_gb300 as nxb
     from nexusbvh_gb300 import scenes
 
     torch.cuda.set_device(local)
-    nxb.load()
+    lib = nxb.load()
     pools = [scenes.uniform_soup(4_194_304, seed=0), scenes.displaced_sphere(2048, 1024, seed=1),
              scenes.clustered(4_194_304, seed=2), scenes.clustered(28_311_552, seed=5)]
     host = [torch.from_numpy(p).pin_memory() for p in pools]
     dev = [t.cuda() for t in host]
-    total = args.warmup + args.steps
-    reqs = served_requests(total)
-    rate = 200.0
-    rng = np.random.default_rng(12)
-    gaps = rng.exponential(1.0 / rate, size=total)
+    del pools
+    stream_ptr = int(torch.cuda.current_stream().cuda_stream)
 
-    def run_pass(on_device: bool):
+    def arrivals_of(gaps):
+        return np.cumsum(gaps)
+
+    def serve(reqs, gaps, warm, on_device):
         srv = nxb.Server(budget_bytes=32 << 30, reserve=True)
-        lat, queue, batched = [], [], 0
-        tickets = []
-        done = threading.Event()
+        results = []
+        tickets_q = _q.Queue()
 
         def drain():
-            nonlocal batched
             for i, t in enumerate(iter(tickets_q.get, None)):
                 r = srv.wait(t)
-                if i >= args.warmup:
-                    lat.append(r.latency_ms)
-                    queue.append(r.queue_ms)
-                    batched += r.batched_with > 1
+                if i >= warm:
+                    results.append((r.latency_ms, r.queue_ms, r.batched_with, r.device_start_ms,
+                                    r.device_end_ms))
                 srv.release(t)
-            done.set()
 
-        import queue as _q
-        tickets_q = _q.Queue()
         th = threading.Thread(target=drain)
         th.start()
         t0 = time.perf_counter()
-        at = t0
+        arr = t0 + arrivals_of(gaps)
         start_timed = None
         for i, (kind, n, kb) in enumerate(reqs):
-            at += gaps[i]
-            wait = at - time.perf_counter()
+            wait = arr[i] - time.perf_counter()
             if wait > 0.0005:
                 time.sleep(wait - 0.0003)  # leave the GIL to the draining thread
-            while time.perf_counter() < at:
+            while time.perf_counter() < arr[i]:
                 pass
-            if i == args.warmup:
+            if i == warm:
                 start_timed = time.perf_counter()
-            src = (dev if on_device else host)[kind][:n]
             cfg = nxb.BuildConfig(prioritize_speed=kb == 30)
-            if on_device:
-                t = srv.submit(src, cfg)
-            else:
-                t = srv.submit(src.numpy(), cfg)
-            tickets.append(t)
+            t = srv.submit(dev[kind][:n] if on_device else host[kind][:n].numpy(), cfg)
             tickets_q.put(t)
         tickets_q.put(None)
         th.join()
         wall = time.perf_counter() - (start_timed or t0)
         st = srv.stats()
         srv.close()
-        tris = sum(n for _, n, _ in reqs[args.warmup:])
-        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                "mean_ms": float(np.mean(lat)), "max_ms": float(np.max(lat)),
-                "queue_p99_ms": float(np.percentile(queue, 99)), "requests": len(lat),
-                "batched_requests": batched, "wall_s": wall, "mtris_s": tris / wall / 1e6,
+        lat = [r[0] for r in results]
+        # jobs (distinct device intervals) whose GPU work overlapped another job's
+        jobs = sorted({(r[3], r[4]) for r in results})
+        overl = sum(1 for k, a in enumerate(jobs) if any(max(a[0], b[0]) < min(a[1], b[1])
+                                                         for b in jobs[max(0, k - 64):k + 64] if b != a))
+        tris = sum(n for _, n, _ in reqs[warm:])
+        return {"p50_ms": _pctl(lat, 50), "p99_ms": _pctl(lat, 99), "mean_ms": float(np.mean(lat)),
+                "max_ms": float(np.max(lat)), "queue_p99_ms": _pctl([r[1] for r in results], 99),
+                "requests": len(lat), "batched_requests": sum(1 for r in results if r[2] > 1),
+                "wall_s": wall, "builds_s": len(lat) / wall, "mtris_s": tris / wall / 1e6,
+                "gpu_jobs": len(jobs), "jobs_overlapping_another": overl,
                 "peak_bytes": int(st.peak_bytes_in_use), "builds": int(st.builds),
                 "batched_builds": int(st.batched_builds)}
 
-    def run_serial():
+    def serial(reqs, gaps, warm, on_device):
         """The same arrivals served by serial plain builds (the reference's
-        model: one nxb_build_bvh8 call at a time, device-resident input)."""
-        lib = nxb.load()
+        model: one nxb_build_bvh8 call at a time), inputs resident on the
+        device or copied from pinned host memory before each build."""
         out = nxb.CBVH8()
-        stream_ptr = int(torch.cuda.current_stream().cuda_stream)
         lat = []
+        d_in = torch.empty((max(n for _, n, _ in reqs), 9), dtype=torch.float32, device="cuda")
         t0 = time.perf_counter()
-        at = t0
-        arrivals = []
-        for g in gaps:
-            at += g
-            arrivals.append(at)
+        arr = t0 + arrivals_of(gaps)
+        start_timed = None
         for i, (kind, n, kb) in enumerate(reqs):
-            while time.perf_counter() < arrivals[i]:
+            while time.perf_counter() < arr[i]:
                 pass
+            if i == warm:
+                start_timed = time.perf_counter()
             c = nxb.BuildConfig(prioritize_speed=kb == 30).to_c()
-            nxb.check(lib.nxb_build_bvh8(dev[kind].data_ptr(), nxb.NXB_PRIM_TRIANGLE, n, ctypes.byref(c),
+            src = dev[kind]
+            if not on_device:
+                d_in[:n].copy_(host[kind][:n], non_blocking=True)
+                src = d_in
+            nxb.check(lib.nxb_build_bvh8(src.data_ptr(), nxb.NXB_PRIM_TRIANGLE, n, ctypes.byref(c),
                                          stream_ptr, ctypes.byref(out), None), "nxb_build_bvh8")
             nxb.check(lib.nxb_free_device_bvh8(ctypes.byref(out)), "nxb_free_device_bvh8")
-            if i >= args.warmup:
-                lat.append((time.perf_counter() - arrivals[i]) * 1e3)
-        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                "mean_ms": float(np.mean(lat)), "max_ms": float(np.max(lat))}
+            if i >= warm:
+                lat.append((time.perf_counter() - arr[i]) * 1e3)
+        wall = time.perf_counter() - (start_timed or t0)
+        tris = sum(n for _, n, _ in reqs[warm:])
+        return {"p50_ms": _pctl(lat, 50), "p99_ms": _pctl(lat, 99), "mean_ms": float(np.mean(lat)),
+                "max_ms": float(np.max(lat)), "wall_s": wall, "builds_s": len(lat) / wall,
+                "mtris_s": tris / wall / 1e6}
 
+    total = warmup + requests
+    reqs = served_requests(total)
+    gaps = np.random.default_rng(12).exponential(1.0 / 200.0, size=total)
+    out = {}
     with ClockSampler(local) as clocks:
-        resident = run_pass(True)
-        hostin = run_pass(False)
-        serial = run_serial()
+        out["device_resident"] = serve(reqs, gaps, warmup, True)
+        out["host_input"] = serve(reqs, gaps, warmup, False)
+        out["serial_plain_device"] = serial(reqs, gaps, warmup, True)
+        out["serial_plain_host"] = serial(reqs, gaps, warmup, False)
+        if burst:
+            breqs = burst_requests(burst + 20)
+            bgaps = np.random.default_rng(22).exponential(1.0 / 20_000.0, size=len(breqs))
+            out["burst"] = serve(breqs, bgaps, 20, True)
+            out["burst_serial_plain"] = serial(breqs, bgaps, 20, True)
+    out["clocks"] = clocks.summary()
+    out["reqs"] = reqs
+    out["warmup"] = warmup
+    del dev, host
+    torch.cuda.empty_cache()
+    return out
+
+
+def served_summary(sv: dict) -> dict:
+    def r(d):
+        return {k: (round(v, 3) if isinstance(v, float) else v) for k, v in d.items()}
+    keys = ["device_resident", "host_input", "serial_plain_device", "serial_plain_host", "burst",
+            "burst_serial_plain"]
+    return {k: r(sv[k]) for k in keys if k in sv}
+
+
+def run_served(args, world, rank, local):
+    """Served form: the served line (p99 latency of device-resident requests)."""
+    sv = measure_served(args, world, rank, local, args.steps, args.warmup)
     if rank != 0:
         return
-    n_big = sum(1 for k, _, _ in reqs[args.warmup:] if k == 3)
+    reqs, warm = sv["reqs"], sv["warmup"]
+    resident, hostin = sv["device_resident"], sv["host_input"]
+    n_big = sum(1 for k, _, _ in reqs[warm:] if k == 3)
     line = {
         "metric": "p99 request latency, served builds (submit -> BVH8 done)",
         "value": round(resident["p99_ms"], 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(resident["mean_ms"], 3), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generators standing in for the reference's scene files)",
-        "config": {"workload": WORKLOADS["served"][0], "requests": args.steps, "big_requests": n_big,
-                   "budget_gib": 32, "streams": 4, "batch_max_prims": 65536,
-                   "l2": "each request's input is streamed once; the big builds exceed L2",
-                   "device_resident": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in resident.items()},
-                   "host_input": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in hostin.items()},
-                   "serial_plain_builds": {k: round(v, 3) for k, v in serial.items()}},
+        "config": dict({"workload": WORKLOADS["served"][0], "requests": args.steps, "big_requests": n_big,
+                        "budget_gib": 32, "streams": 4, "batch_max_prims": 65536,
+                        "l2": "each request's input is streamed once; the big builds exceed L2",
+                        "burst": "1,000 requests of configuration-0/1 meshes (n log-U[1024, 65536], 30-bit) "
+                                 "arriving at 20,000/s"},
+                       **served_summary(sv)),
         "roofline": None,
         "e2e": {"value": round(hostin["p99_ms"], 3), "unit": "ms",
-                "h2d_bytes_per_step": int(np.mean([n * 36 for _, n, _ in reqs[args.warmup:]])),
+                "h2d_bytes_per_step": int(np.mean([n * 36 for _, n, _ in reqs[warm:]])),
                 "d2h_bytes_per_step": 40,
                 "call": "nxb_server_submit with host (pinned) input, nxb_server_wait, nxb_server_release"},
         "gpu_launches": None,
-        "clocks": clocks.summary(),
+        "clocks": sv["clocks"],
     }
     print(json.dumps(line), flush=True)
 
@@ -787,6 +895,8 @@ def main():
                     help="batched workloads: leave out the loop-of-plain-builds comparison")
     ap.add_argument("--no-autotune", action="store_true",
                     help="batched workloads: build with the default tuning instead of tuning first")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="plain workloads: leave out the batched and served records of the line")
     args = ap.parse_args()
     if args.key_bits is None:
         args.key_bits = WORKLOADS[args.workload][1]

@@ -490,6 +490,13 @@ typedef struct nxb_server_result {
     uint32_t batched_with;  /* meshes in the build that produced it (1 = built alone) */
     double queue_ms;        /* submit -> launch (host clock) */
     double latency_ms;      /* submit -> completion seen by the server (host clock) */
+    /* The build's work on the GPU, in milliseconds since the server was
+     * created, from events recorded on its stream before its first operation
+     * (the input copy or the build) and after its last (the result copies):
+     * requests whose intervals intersect had work on the GPU at the same
+     * time.  Requests built together share one interval. */
+    double device_start_ms;
+    double device_end_ms;
 } nxb_server_result;
 
 typedef struct nxb_server_stats {

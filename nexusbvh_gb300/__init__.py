@@ -110,7 +110,8 @@ class CServerConfig(ctypes.Structure):
 
 class CServerResult(ctypes.Structure):
     _fields_ = [("bvh8", CBVH8), ("status", ctypes.c_int32), ("batched_with", ctypes.c_uint32),
-                ("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
+                ("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+                ("device_start_ms", ctypes.c_double), ("device_end_ms", ctypes.c_double)]
 
 
 class CServerStats(ctypes.Structure):

@@ -48,6 +48,7 @@ struct Request {
     size_t scratch_bytes = 0;  // input copy + workspace + BVH2, freed after the build
     size_t result_bytes = 0;   // BVH8 nodes + primIdx, freed on release
     Clock::time_point t_submit, t_start, t_done;
+    double dev_start_ms = 0.0, dev_end_ms = 0.0;  // since the server's base event
     unsigned char* result = nullptr;
     nxb_bvh8 bvh8{};
     nxb_status status = NXB_OK;
@@ -73,6 +74,7 @@ struct Job {
 // Pinned per-slot staging: a slot runs one job at a time.
 struct Slot {
     cudaStream_t stream = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_end = nullptr;  // the running job's device interval
     Job* job = nullptr;
     nxb_build_result* h_result = nullptr;  // plain builds
     uint32_t* h_err = nullptr;             // batched builds
@@ -89,6 +91,7 @@ using namespace nxb;
 struct nxb_server {
     nxb_server_config cfg{};
     int device = 0;
+    cudaEvent_t base = nullptr;  // device time zero of the request intervals
     cudaMemPool_t pool = nullptr;
     cudaStream_t release_stream = nullptr;
     std::vector<Slot> slots;
@@ -154,6 +157,8 @@ nxb_status launch_plain(nxb_server* s, Job* j) {
     if (e) return record_cuda_error(e);
     size_t at = 0;
     const void* prims = r->prims;
+    e = cudaEventRecord(sl->ev_start, st);
+    if (e) return record_cuda_error(e);
     if (!r->on_device) {
         prims = scratch;
         e = cudaMemcpyAsync(scratch, r->prims, prim_bytes(r->type) * r->n, cudaMemcpyHostToDevice, st);
@@ -170,6 +175,7 @@ nxb_status launch_plain(nxb_server* s, Job* j) {
     nxb_status stt = nxb_build_async(prims, r->type, r->n, &r->cfg, ws, sz.workspace_bytes, b2, b8, prim, d_res, st);
     if (stt != NXB_OK) return stt;
     e = cudaMemcpyAsync(sl->h_result, d_res, sizeof(nxb_build_result), cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaEventRecord(sl->ev_end, st);
     if (!e) e = cudaFreeAsync(scratch, st);
     if (!e) j->scratch = nullptr;
     if (!e) e = cudaLaunchHostFunc(st, on_job_done, j);
@@ -196,6 +202,7 @@ nxb_status launch_batch(nxb_server* s, Job* j) {
     for (uint32_t m = 0; m < M && !e; ++m) e = alloc(s, (void**)&j->reqs[m]->result, j->reqs[m]->result_bytes, st);
     if (e) return record_cuda_error(e);
     batch_bind(scratch + in_bytes, &a);
+    e = cudaEventRecord(sl->ev_start, st);
     // the meshes end to end
     for (uint32_t m = 0; m < M && !e; ++m) {
         const Request* r = j->reqs[m];
@@ -224,6 +231,7 @@ nxb_status launch_batch(nxb_server* s, Job* j) {
         r->bvh8.prim_count = r->n;
     }
     if (!e) e = cudaMemcpyAsync(sl->h_meshes, a.results, sizeof(nxb_batch_mesh) * M, cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaEventRecord(sl->ev_end, st);
     if (!e) e = cudaFreeAsync(scratch, st);
     if (!e) j->scratch = nullptr;
     if (!e) e = cudaLaunchHostFunc(st, on_job_done, j);
@@ -247,8 +255,15 @@ void reap(nxb_server* s, Slot& sl) {
         r->bvh8.node_count = sl.h_result->bvh8_node_count;
         r->bvh8.bounds = sl.h_result->scene_bounds;
     }
+    // the job's events have completed (its host function ran after them)
+    float t0 = 0.f, t1 = 0.f;
+    if (cudaEventElapsedTime(&t0, s->base, sl.ev_start) != cudaSuccess ||
+        cudaEventElapsedTime(&t1, s->base, sl.ev_end) != cudaSuccess)
+        t0 = t1 = -1.f;
     for (Request* r : j->reqs) {
         r->t_done = j->t_done;
+        r->dev_start_ms = t0;
+        r->dev_end_ms = t1;
         r->done = true;
         r->batched_with = (uint32_t)j->reqs.size();
         if (r->status != NXB_OK && r->result) {
@@ -381,6 +396,8 @@ void destroy_server(nxb_server* s) {
     if (s->release_stream) cudaStreamSynchronize(s->release_stream);
     for (Slot& sl : s->slots) {
         if (sl.stream) cudaStreamDestroy(sl.stream);
+        if (sl.ev_start) cudaEventDestroy(sl.ev_start);
+        if (sl.ev_end) cudaEventDestroy(sl.ev_end);
         if (sl.h_result) cudaFreeHost(sl.h_result);
         if (sl.h_err) cudaFreeHost(sl.h_err);
         if (sl.h_off) cudaFreeHost(sl.h_off);
@@ -388,6 +405,7 @@ void destroy_server(nxb_server* s) {
         if (sl.h_meshes) cudaFreeHost(sl.h_meshes);
     }
     if (s->release_stream) cudaStreamDestroy(s->release_stream);
+    if (s->base) cudaEventDestroy(s->base);
     if (s->pool) cudaMemPoolDestroy(s->pool);
     delete s;
 }
@@ -398,6 +416,8 @@ void fill_result(const Request* r, nxb_server_result* out) {
     out->batched_with = r->batched_with;
     out->queue_ms = std::chrono::duration<double, std::milli>(r->t_start - r->t_submit).count();
     out->latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+    out->device_start_ms = r->dev_start_ms;
+    out->device_end_ms = r->dev_end_ms;
 }
 
 // One tiny build through each pipeline a server runs at the default radius:
@@ -485,6 +505,8 @@ nxb_status nxb_server_create(const nxb_server_config* config, nxb_server** out) 
     s->slots.resize(c.streams);
     for (Slot& sl : s->slots) {
         if (!e) e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+        if (!e) e = cudaEventCreate(&sl.ev_start);
+        if (!e) e = cudaEventCreate(&sl.ev_end);
         if (!e) e = cudaMallocHost(&sl.h_result, sizeof(nxb_build_result));
         if (!e) e = cudaMallocHost(&sl.h_err, sizeof(uint32_t));
         if (!e) e = cudaMallocHost(&sl.h_off, 4ull * (c.batch_max_meshes + 1));
@@ -508,6 +530,14 @@ nxb_status nxb_server_create(const nxb_server_config* config, nxb_server** out) 
     if (wst != NXB_OK) {
         destroy_server(s);
         return wst;
+    }
+    e = cudaEventCreate(&s->base);
+    if (!e) e = cudaEventRecord(s->base, s->release_stream);
+    if (!e) e = cudaEventSynchronize(s->base);
+    if (e) {
+        const nxb_status st = record_cuda_error(e);
+        destroy_server(s);
+        return st;
     }
     s->worker = std::thread(worker_main, s);
     *out = s;

@@ -131,6 +131,47 @@ def test_server_mixed_batch_matches_oracle(gpu, orc):
     srv.close()
 
 
+def intervals_overlap(a, b):
+    return max(a.device_start_ms, b.device_start_ms) < min(a.device_end_ms, b.device_end_ms)
+
+
+def test_server_requests_overlap_on_the_device(gpu, orc):
+    """Continuous batching runs requests at the same time: with four stream
+    slots, requests submitted together have GPU work at the same time (their
+    device intervals, from events on their streams, intersect), and each
+    result is still the mesh's plain build.  Requests built together share
+    one interval."""
+    srv = nxb.Server(streams=4, batch_max_prims=1)  # every request its own build
+    meshes = [scenes.clustered(400_000 + 10_000 * i, seed=90 + i) for i in range(8)]
+    tickets = [srv.submit(S.dev(m), nxb.BuildConfig()) for m in meshes]
+    res = []
+    for t, m in zip(tickets, meshes):
+        r = srv.wait(t)
+        assert 0.0 <= r.device_start_ms < r.device_end_ms
+        check_same(orc, r, m, 63)
+        res.append(r)
+        srv.release(t)
+    srv.close()
+    pairs = [(i, j) for i in range(len(res)) for j in range(i + 1, len(res)) if intervals_overlap(res[i], res[j])]
+    assert pairs, "no two requests had work on the GPU at the same time"
+
+    srv = nxb.Server(streams=1)
+    t_big = srv.submit(scenes.clustered(1_000_000, seed=5), nxb.BuildConfig(prioritize_speed=True))
+    small = [srv.submit(scenes.uniform_soup(500 + 100 * i, seed=i), nxb.BuildConfig(prioritize_speed=True))
+             for i in range(6)]
+    srv.wait(t_big)
+    srv.release(t_big)
+    rs = []
+    for t in small:
+        rs.append(srv.wait(t))
+    together = [r for r in rs if r.batched_with > 1]
+    assert len(together) >= 2
+    assert all(r.device_start_ms == together[0].device_start_ms for r in together[:2])
+    for t in small:
+        srv.release(t)
+    srv.close()
+
+
 def test_server_admission_and_budget(gpu, orc):
     budget = 96 << 20
     srv = nxb.Server(budget_bytes=budget, streams=4, batch_max_prims=1)  # no batching: plain builds only
