@@ -60,6 +60,7 @@ def load() -> ctypes.CDLL:
             "orc_digest_bvh2": (ctypes.c_uint64, [P, U, U]),
             "orc_digest_bvh8": (ctypes.c_uint64, [P, U, P, U]),
             "orc_find_nn": (None, [U, P, U, P]),
+            "orc_auction": (ctypes.c_int, [P, P, U, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)

@@ -17,6 +17,11 @@ is not used: this script compiles the sources directly.
             (--use_fast_math -rdc=true; arch sm_103, which is what `native` resolves to
             on GB300) plus oracle/ref_harness.cpp into
             oracle/_ref/libnxbref_r{4,8,16}.so, one per search radius.
+  build_auction():  copies the reference's auction slot assignment
+            (AuctionAssignment, the USE_AUCTION cost table of the BVH8
+            kernel, the nibble helpers) verbatim into oracle/_ref/*.inc and
+            compiles them as host code with oracle/ref_auction.cpp into
+            oracle/_ref/libref_auction.so (g++ only; no GPU involved).
 """
 from __future__ import annotations
 
@@ -130,5 +135,61 @@ def build(force: bool = False) -> list[Path]:
     return libs
 
 
+def _braced(text: str, start: int) -> int:
+    """Index just past the brace block that opens at or after `start`."""
+    i = text.index("{", start)
+    depth = 0
+    for k in range(i, len(text)):
+        if text[k] == "{":
+            depth += 1
+        elif text[k] == "}":
+            depth -= 1
+            if depth == 0:
+                return k + 1
+    raise RuntimeError("unbalanced braces")
+
+
+def auction_lib() -> Path:
+    return REF_OUT / "libref_auction.so"
+
+
+def build_auction(force: bool = False) -> Path | None:
+    """The reference's auction assignment as a host library (see above);
+    None when the reference's sources are not available."""
+    if not stage():
+        return None
+    wide = (STAGE / "NexusBVH/src/Cuda/WideConverter.cu").read_text()
+    utils = (STAGE / "NexusBVH/src/Cuda/BuilderUtils.h").read_text()
+    # the file's constants (INVALID_ASSIGNMENT, THETA, MAX_COST, invTheta, ...)
+    # then GetCost (both overloads), ComputeAssignmentCost, AuctionAssignment
+    p0 = wide.index("#define INVALID_ASSIGNMENT")
+    p1 = wide.index("namespace NXB", p0)
+    a = wide.index("__device__ __forceinline__ float GetCost(uint32_t s, float3 offset)")
+    b = _braced(wide, wide.index("void AuctionAssignment("))
+    functions = "}  // namespace NXB\n" + wide[p0:p1] + "namespace NXB {\n" + wide[a:b]
+    # the kernel's cost table and call, from its parent centroid to the call
+    c = wide.index("float3 parentCentroid =")
+    d = wide.index("#else", wide.index("#ifdef USE_AUCTION", c))
+    table = "\n".join(line for line in wide[c:d].splitlines() if not line.strip().startswith("#ifdef"))
+    e = utils.index("__device__ __forceinline__ uint32_t GetNibble(")
+    f = _braced(utils, utils.index("void SetNibble(", e))
+    nibbles = utils[e:f]
+    REF_OUT.mkdir(parents=True, exist_ok=True)
+    outs = {"auction_functions.inc": functions, "auction_cost_table.inc": table, "auction_nibbles.inc": nibbles}
+    changed = force or not auction_lib().exists()
+    for name, body in outs.items():
+        p = REF_OUT / name
+        if not p.exists() or p.read_text() != body:
+            p.write_text(body)
+            changed = True
+    src = ORACLE_DIR / "ref_auction.cpp"
+    if changed or src.stat().st_mtime > auction_lib().stat().st_mtime:
+        cxx = os.environ.get("CXX", "g++")
+        _run([cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+              "-I", str(ORACLE_DIR), "-o", str(auction_lib()), str(src)])
+    return auction_lib()
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv))
+    print(build_auction(force="--force" in sys.argv))

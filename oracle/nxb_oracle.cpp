@@ -917,6 +917,30 @@ uint8_t orc_f2u8(float x) { return f2u8(x); }
 
 // Lane-by-lane FindNearestNeighbor for one warp: boxes32 holds 32 boxes
 // (6 floats each), the first `num` active.
+// The auction slot assignment of one BVH8 node: the parent's box and
+// `count` (1..8) child boxes, 6 floats each.  Returns 1 and the nibble-packed
+// assignment, or 0 where the oracle falls back to the greedy assignment
+// (bid limit, or a bid with no finite reward).
+int orc_auction(const float* parent6, const float* child6, uint32_t count, uint32_t* out) {
+    if (count == 0 || count > 8) return 0;
+    Node2 nodes[8];
+    uint32_t child[8];
+    for (uint32_t c = 0; c < count; ++c) {
+        for (int a = 0; a < 3; ++a) {
+            nodes[c].b.mn[a] = child6[6 * c + a];
+            nodes[c].b.mx[a] = child6[6 * c + 3 + a];
+        }
+        nodes[c].left = nodes[c].right = kInvalid;
+        child[c] = c;
+    }
+    Box pb;
+    for (int a = 0; a < 3; ++a) {
+        pb.mn[a] = parent6[a];
+        pb.mx[a] = parent6[3 + a];
+    }
+    return auction(pb, child, count, nodes, out) ? 1 : 0;
+}
+
 void orc_find_nn(uint32_t num, const float* boxes32, uint32_t radius, uint32_t* nn32) {
     Box cb[32];
     std::memcpy(cb, boxes32, sizeof(cb));
