@@ -174,7 +174,7 @@ def test_server_argument_checks_need_no_device(lib):
     assert lib.nxb_server_wait(None, 1, None) == 1
     assert lib.nxb_server_release(None, 1) == 1
     assert lib.nxb_server_destroy(None) == 1
-    assert ctypes.sizeof(nxb.CServerResult) == 80 and ctypes.sizeof(nxb.CServerStats) == 64
+    assert ctypes.sizeof(nxb.CServerResult) == 96 and ctypes.sizeof(nxb.CServerStats) == 64
 
 
 def test_validator_wrappers_check_tensors():
