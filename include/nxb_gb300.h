@@ -413,7 +413,7 @@ typedef struct nxb_batch_arrays {      /* device views owned by the batch */
 } nxb_batch_arrays;
 
 typedef struct nxb_batch_tuning {
-    uint32_t sort_digit_bits;   /* 5..8: bits per radix sort pass */
+    uint32_t sort_digit_bits;   /* 4..8: bits per radix sort pass (at most 10 passes) */
     uint32_t search_radius;     /* H-PLOC radius in use */
     uint32_t hploc_ctas_per_sm; /* cap on the H-PLOC persistent grid (0 = occupancy) */
     uint32_t fusion_groups;     /* BVH2/BVH8 fusion point: 0 or 1 = collapse after H-PLOC has built

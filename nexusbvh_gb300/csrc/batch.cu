@@ -80,7 +80,7 @@ Segments segments_of(const BatchArena& a) {
 uint32_t batch_bvh8_capacity(uint32_t n) { return n == 0 ? 1u : (uint32_t)(((size_t)4 * n - 1 + 6) / 7); }
 
 bool batch_digit_ok(uint32_t mesh_bits, uint32_t d) {
-    if (d < 5 || d > 8) return false;
+    if (d < 4 || d > 8) return false;
     return (30 + mesh_bits + d - 1) / d <= (uint32_t)kMaxSortPasses;
 }
 
@@ -431,7 +431,7 @@ nxb_status nxb_batch_autotune(nxb_batch* b, const void* prims, uint32_t flags, u
     const nxb_batch_tuning start = b->tuning;
     std::vector<nxb_batch_tuning> cand;
     for (uint32_t r : radii)
-        for (uint32_t d : {8u, 7u, 6u, 5u}) {
+        for (uint32_t d : {8u, 7u, 6u, 5u, 4u}) {
             if (!batch_digit_ok(b->arena.mesh_bits, d)) continue;
             for (uint32_t c : {0u, 4u})
                 for (uint32_t g : {1u, 2u, 4u})

@@ -12,7 +12,9 @@
 
 namespace nxb {
 
-constexpr int kMaxSortPasses = 8;
+// Most passes of a sort plan: 10 for the batched 4-bit plan over 40-bit
+// keys (30-bit codes and a 10-bit mesh index).
+constexpr int kMaxSortPasses = 10;
 
 // BVH8 work-queue counters, each on its own 128-byte line (they are polled
 // and bumped by every warp): next slot to claim, BVH8 nodes, leaves, work

@@ -755,12 +755,14 @@ namespace {
 
 constexpr size_t kNoAllocAlign = 256;
 constexpr size_t align_na(size_t x) { return (x + kNoAllocAlign - 1) / kNoAllocAlign * kNoAllocAlign; }
-constexpr size_t kNoAllocHist = align_na(sizeof(uint32_t) * nxb::kMaxSortPasses * nxb::kRadixBins);
-constexpr size_t kNoAllocCtr = align_na(sizeof(uint32_t) * nxb::kMaxSortPasses);
+// 8-bit digits: at most 8 passes over a 64-bit key
+constexpr int kNoAllocPasses = 8;
+constexpr size_t kNoAllocHist = align_na(sizeof(uint32_t) * kNoAllocPasses * nxb::kRadixBins);
+constexpr size_t kNoAllocCtr = align_na(sizeof(uint32_t) * kNoAllocPasses);
 // one look-back word per (tile, digit, pass); the 64-bit tile is the smaller one
 constexpr size_t kNoAllocTiles =
     (NXB_NOALLOC_SORT_MAX_COUNT + nxb::tile_keys<uint64_t>() - 1) / nxb::tile_keys<uint64_t>();
-constexpr size_t kNoAllocLookback = align_na(4ull * kNoAllocTiles * nxb::kRadixBins * nxb::kMaxSortPasses);
+constexpr size_t kNoAllocLookback = align_na(4ull * kNoAllocTiles * nxb::kRadixBins * kNoAllocPasses);
 constexpr size_t kNoAllocKeys = align_na(8ull * NXB_NOALLOC_SORT_MAX_COUNT);
 constexpr size_t kNoAllocVals = align_na(4ull * NXB_NOALLOC_SORT_MAX_COUNT);
 constexpr size_t kNoAllocZeroed = kNoAllocHist + kNoAllocCtr + kNoAllocLookback;

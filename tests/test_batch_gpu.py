@@ -35,9 +35,11 @@ def plain(prims_m, radius=8):
     return b2, b8, prim, out.bounds
 
 
-def check_against_plain(batch, meshes, prims, counts, orc, radius=8):
+def check_against_plain(batch, meshes, prims, counts, orc, radius=8, only=None):
     off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
     for m, n in enumerate(counts):
+        if only is not None and m not in only:
+            continue
         info = meshes[m]
         assert info.prim_offset == off[m] and info.prim_count == n
         if n == 0:
@@ -142,7 +144,8 @@ def test_batch_replay_and_tuning_keep_results(gpu, orc):
     first = batch.build(d)
     ref = [(batch.mesh_bvh2_host(m, first).tobytes(), batch.mesh_bvh8_host(m)) for m in range(len(counts))
            if counts[m]]
-    for digits, ctas, groups, block in ((5, 0, 1, 128), (6, 4, 2, 512), (7, 0, 4, 256), (8, 4, 1, 512)):
+    for digits, ctas, groups, block in ((4, 0, 2, 128), (5, 0, 1, 128), (6, 4, 2, 512), (7, 0, 4, 256),
+                                        (8, 4, 1, 512)):
         t = batch.tuning()
         t.sort_digit_bits, t.hploc_ctas_per_sm, t.fusion_groups, t.block_size = digits, ctas, groups, block
         batch.set_tuning(t)
@@ -186,6 +189,27 @@ def test_batch_arguments(gpu):
     assert lib.nxb_batch_create(1, ok.ctypes.data, 0, ctypes.byref(c), ctypes.byref(h)) == 1
     b = nxb.Batch([10, 10])
     t = b.tuning()
-    t.sort_digit_bits = 4
+    t.sort_digit_bits = 3
     with pytest.raises(nxb.NxbError):
         b.set_tuning(t)
+
+
+def test_batch_ten_pass_plan(gpu, orc):
+    """1,024 meshes make 40-bit batch keys (30-bit codes, 10-bit mesh
+    index): 4-bit digits sort them in 10 passes, 8-bit digits in 5; every
+    mesh's trees are the same either way."""
+    rng = np.random.default_rng(17)
+    counts = [int(x) for x in rng.integers(0, 300, size=1024)]
+    prims = make_batch(counts, seed=17)
+    d = S.dev(prims)
+    batch = nxb.Batch(counts)
+    eight = batch.build(d)
+    ref = [batch.mesh_bvh2_host(m, eight).tobytes() for m in range(len(counts)) if counts[m]]
+    t = batch.tuning()
+    t.sort_digit_bits = 4
+    batch.set_tuning(t)
+    four = batch.build(d)
+    got = [batch.mesh_bvh2_host(m, four).tobytes() for m in range(len(counts)) if counts[m]]
+    assert got == ref
+    k = next(m for m in range(len(counts)) if counts[m] > 100)
+    check_against_plain(batch, four, prims, counts, orc, only=[k])
