@@ -56,7 +56,7 @@ struct Layout {
     SortPlan plan{};
     size_t tiles_words = 0;  // look-back words for all passes
     size_t ctrl = 0, result = 0, cost = 0, keys_a = 0, keys_b = 0, vals_a = 0, vals_b = 0, lookback = 0, parent = 0,
-           pairs = 0, total = 0;
+           pairs = 0, records = 0, total = 0;
 };
 
 Layout make_layout(uint32_t n, uint32_t key_bits) {
@@ -86,6 +86,7 @@ Layout make_layout(uint32_t n, uint32_t key_bits) {
     L.lookback = seg(4ull * L.tiles_words);
     L.parent = seg(4ull * n);
     L.pairs = seg(8ull * n);
+    L.records = seg(32ull * n);
     L.total = off;
     return L;
 }
@@ -195,7 +196,8 @@ nxb_status enqueue_build(const void* prims, nxb_prim_type type, uint32_t n, cons
     NXB_TRY(mark(3));
     // the sort's second value buffer holds the H-PLOC cluster tokens
     NXB_TRY(launch_hploc(L.key_bytes, keys_a, vals_a, parent, bvh2, n, radius_of(cfg), vals_b,
-                         &ctrl->parent_of_last, &ctrl->hploc_leaf_ctr, &ctrl->error_word, s));
+                         &ctrl->parent_of_last, &ctrl->hploc_leaf_ctr, &ctrl->error_word, s,
+                         reinterpret_cast<Node2*>(ws + L.records)));
     NXB_TRY(mark(4));
     if (bvh8) {
         NXB_TRY(launch_bvh8_init(pairs, n, ctrl->bvh8_ctr, s));
@@ -720,8 +722,8 @@ nxb_status nxb_stage_radix_sort(uint32_t key_bytes, const void* d_keys_in, void*
     return NXB_OK;
 }
 
-// parent slots (4n) | cluster tokens (4n) | 2 counters
-size_t nxb_hploc_scratch_bytes(uint32_t n) { return 2 * align_up(4ull * n) + kAlign; }
+// parent slots (4n) | cluster tokens (4n) | 2 counters | cluster records (32n)
+size_t nxb_hploc_scratch_bytes(uint32_t n) { return 2 * align_up(4ull * n) + kAlign + align_up(32ull * n); }
 
 nxb_status nxb_stage_hploc(uint32_t key_bytes, const void* d_sorted_keys, uint32_t* d_cluster_idx,
                            nxb_bvh2_node* d_nodes, uint32_t n, uint32_t search_radius, void* d_scratch,
@@ -739,8 +741,9 @@ nxb_status nxb_stage_hploc(uint32_t key_bytes, const void* d_sorted_keys, uint32
     NXB_TRY(launch_fill_u32(parent, kInvalid, n, stream));
     NXB_TRY(launch_fill_u32(words, kInvalid, 1, stream));  // parent_of_last
     NXB_TRY(launch_fill_u32(words + 1, 0, 1, stream));      // leaf counter
+    Node2* records = reinterpret_cast<Node2*>(base + 2 * align_up(4ull * n) + kAlign);
     NXB_TRY(launch_hploc(key_bytes, d_sorted_keys, d_cluster_idx, parent, reinterpret_cast<Node2*>(d_nodes), n,
-                         search_radius, tokens, words, words + 1, d_error_word, stream));
+                         search_radius, tokens, words, words + 1, d_error_word, stream, records));
     return NXB_OK;
 }
 

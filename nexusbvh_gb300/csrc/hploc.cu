@@ -191,6 +191,7 @@ __device__ __forceinline__ uint32_t nearest_neighbour(uint32_t num, const Box& c
 struct MergeCtx {
     Node2* nodes;
     uint32_t* tok;             // first-leaf token of each stored cluster
+    Node2* rec;                // if not null: stored clusters as {box, id, token} records
     uint32_t* parent_of_last;  // node whose child is node 2n-2 (root fix-up)
     uint32_t n;
     uint32_t node_limit;       // 2n-1
@@ -292,8 +293,8 @@ __device__ __forceinline__ MergeCtx mesh_ctx(const MergeCtx& all, const Seg& seg
         const uint32_t mesh = __shfl_sync(kFullMask, me.m, owner);
         start = __shfl_sync(kFullMask, me.start, owner);
         const uint32_t count = __shfl_sync(kFullMask, me.count, owner);
-        return MergeCtx{all.nodes + 2ull * start, all.tok, all.parent_of_last + mesh, count, 2 * count - 1, all.err,
-};
+        return MergeCtx{all.nodes + 2ull * start, all.tok, all.rec, all.parent_of_last + mesh, count, 2 * count - 1,
+                        all.err};
     } else {
         start = 0;
         return all;
@@ -303,7 +304,7 @@ __device__ __forceinline__ MergeCtx mesh_ctx(const MergeCtx& all, const Seg& seg
 // PlocMerge (BinaryBuilder.cu:200-273, the merge part) for the range of
 // lane `owner`; `start` is the first sorted position of its mesh and m
 // addresses that mesh's nodes.
-template <int R, bool COVER>
+template <int R, bool COVER, bool REC>
 __device__ __forceinline__ void merge_windows(uint32_t owner, uint32_t left, uint32_t right, uint32_t split,
                                               bool final, uint32_t start, uint32_t* cluster, const MergeCtx& m) {
     const uint32_t lane = lane_id();
@@ -321,16 +322,35 @@ __device__ __forceinline__ void merge_windows(uint32_t owner, uint32_t left, uin
     const uint32_t l_size = min(l_len, kMergeThreshold);
     const uint32_t r_size = min(r_len, kMergeThreshold);
     uint32_t v = kInvalid, t = kInvalid;
-    if (lane < 16) {
-        if (lane < l_size) {
-            const uint32_t pos = l_start + lane;
-            v = __ldcg(cluster + pos);
-            t = l_len > kMergeThreshold ? __ldcg(m.tok + pos) : pos - start;
+    Box wb;  // REC: the window's box at its position, before compaction
+    wb.mn = make_float3(0.f, 0.f, 0.f);
+    wb.mx = wb.mn;
+    {
+        const bool lo = lane < 16;
+        const uint32_t k = lo ? lane : lane - 16;
+        if (k < (lo ? l_size : r_size)) {
+            const uint32_t pos = (lo ? l_start : mid) + k;
+            const bool stored = (lo ? l_len : r_len) > kMergeThreshold;
+            if constexpr (REC) {
+                if (stored) {
+                    // a stored window: id, token and box in one record, 16
+                    // consecutive records per window
+                    const uint4* p = reinterpret_cast<const uint4*>(m.rec + pos);
+                    const uint4 a = __ldcg(p), b = __ldcg(p + 1);
+                    wb.mn = make_float3(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z));
+                    wb.mx = make_float3(__uint_as_float(a.w), __uint_as_float(b.x), __uint_as_float(b.y));
+                    v = b.z;
+                    t = b.w;
+                } else {
+                    v = __ldcg(cluster + pos);
+                    t = pos - start;
+                    if (v < m.node_limit) wb = load_box_cg(m.nodes, v);
+                }
+            } else {
+                v = __ldcg(cluster + pos);
+                t = stored ? __ldcg(m.tok + pos) : pos - start;
+            }
         }
-    } else if (lane - 16 < r_size) {
-        const uint32_t pos = mid + lane - 16;
-        v = __ldcg(cluster + pos);
-        t = r_len > kMergeThreshold ? __ldcg(m.tok + pos) : pos - start;
     }
     const uint32_t vb = __ballot_sync(kFullMask, v != kInvalid);
     const uint32_t num_left = __popc(vb & 0xFFFFu), num_right = __popc(vb >> 16);
@@ -348,11 +368,19 @@ __device__ __forceinline__ void merge_windows(uint32_t owner, uint32_t left, uin
         return;
     }
     Box cb;
-    if (lane < num) {
-        cb = load_box_cg(m.nodes, cid);
+    if constexpr (REC) {
+        cb = shfl_box(wb, src);
+        if (lane >= num) {
+            cb.mn = make_float3(0.f, 0.f, 0.f);
+            cb.mx = cb.mn;
+        }
     } else {
-        cb.mn = make_float3(0.f, 0.f, 0.f);
-        cb.mx = cb.mn;
+        if (lane < num) {
+            cb = load_box_cg(m.nodes, cid);
+        } else {
+            cb.mn = make_float3(0.f, 0.f, 0.f);
+            cb.mx = cb.mn;
+        }
     }
     const uint32_t threshold = fin ? 1u : kMergeThreshold;
     while (num > threshold) {
@@ -366,8 +394,15 @@ __device__ __forceinline__ void merge_windows(uint32_t owner, uint32_t left, uin
     }
     // StoreIndices (BinaryBuilder.cu:59-69)
     if (lane < num_left + num_right) {
-        __stcg(cluster + l_start + lane, cid);
-        __stcg(m.tok + l_start + lane, ctok);
+        if constexpr (REC) {
+            uint4* p = reinterpret_cast<uint4*>(m.rec + l_start + lane);
+            __stcg(p, make_uint4(__float_as_uint(cb.mn.x), __float_as_uint(cb.mn.y), __float_as_uint(cb.mn.z),
+                                 __float_as_uint(cb.mx.x)));
+            __stcg(p + 1, make_uint4(__float_as_uint(cb.mx.y), __float_as_uint(cb.mx.z), cid, ctok));
+        } else {
+            __stcg(cluster + l_start + lane, cid);
+            __stcg(m.tok + l_start + lane, ctok);
+        }
     }
 }
 
@@ -380,9 +415,9 @@ __device__ __forceinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32
     if constexpr (Seg::kBatch) {
         uint32_t start;
         const MergeCtx m = mesh_ctx<Seg>(all, seg, me, owner, start);
-        merge_windows<R, false>(owner, left, right, split, final, start, cluster, m);
+        merge_windows<R, false, false>(owner, left, right, split, final, start, cluster, m);
     } else {
-        merge_windows<R, true>(owner, left, right, split, final, 0u, cluster, all);
+        merge_windows<R, true, true>(owner, left, right, split, final, 0u, cluster, all);
     }
 }
 
@@ -426,9 +461,9 @@ template <typename K, int R, typename Seg>
 __global__ __launch_bounds__(kThreads, hploc_ctas_per_sm<R, Seg>()) void hploc_kernel(const K* __restrict__ keys, uint32_t* cluster,
                                                          uint32_t* parent, Node2* nodes, Seg seg, uint32_t begin,
                                                          uint32_t* tok, uint32_t* parent_of_last, uint32_t* leaf_ctr,
-                                                         uint32_t* err, uint32_t end, uint32_t chunk) {
+                                                         uint32_t* err, uint32_t end, uint32_t chunk, Node2* rec) {
     const uint32_t lane = lane_id();
-    const MergeCtx all{nodes, tok, parent_of_last, end, 2 * end - 1, err};
+    const MergeCtx all{nodes, tok, rec, parent_of_last, end, 2 * end - 1, err};
     uint32_t left = 0, right = 0, split = 0;
     // the lane's mesh; a plain build has one, known at compile time
     MeshSpan me = Seg::kBatch ? MeshSpan{0, 0, 0} : seg.of_prim(0);
@@ -503,7 +538,7 @@ __global__ __launch_bounds__(kThreads, hploc_ctas_per_sm<R, Seg>()) void hploc_k
 template <typename K, int R, typename Seg>
 cudaError_t launch_r(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, Seg seg, uint32_t begin,
                      uint32_t end, uint32_t* tok, uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err,
-                     uint32_t max_per_sm, cudaStream_t s) {
+                     uint32_t max_per_sm, cudaStream_t s, Node2* rec) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hploc_kernel<K, R, Seg>, kThreads, 0);
     if (max_per_sm && (uint32_t)per_sm > max_per_sm) per_sm = (int)max_per_sm;
@@ -512,24 +547,24 @@ cudaError_t launch_r(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* 
     const uint32_t grid = std::max(1u, std::min(want, (uint32_t)(device_info().sms * per_sm)));
     const uint32_t chunk = leaf_chunk(end - begin, grid * (kThreads / 32), Seg::kBatch);
     hploc_kernel<K, R, Seg><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, seg, begin, tok, pol, leaf_ctr,
-                                                      err, end, chunk);
+                                                      err, end, chunk, rec);
     return cudaGetLastError();
 }
 
 template <typename K, typename Seg>
 cudaError_t launch_t(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, Seg seg, uint32_t begin,
                      uint32_t end, uint32_t radius, uint32_t* tok, uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err,
-                     uint32_t max_per_sm, cudaStream_t s) {
+                     uint32_t max_per_sm, cudaStream_t s, Node2* rec = nullptr) {
     switch (radius) {
         case 4:
             return launch_r<K, 4>(keys, cluster, parent, nodes, seg, begin, end, tok, pol, leaf_ctr, err, max_per_sm,
-                                  s);
+                                  s, rec);
         case 16:
             return launch_r<K, 16>(keys, cluster, parent, nodes, seg, begin, end, tok, pol, leaf_ctr, err,
-                                   max_per_sm, s);
+                                   max_per_sm, s, rec);
         default:
             return launch_r<K, 8>(keys, cluster, parent, nodes, seg, begin, end, tok, pol, leaf_ctr, err, max_per_sm,
-                                  s);
+                                  s, rec);
     }
 }
 
@@ -537,13 +572,13 @@ cudaError_t launch_t(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* 
 
 cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
                          uint32_t n, uint32_t radius, uint32_t* tokens, uint32_t* parent_of_last, uint32_t* leaf_ctr,
-                         uint32_t* err, cudaStream_t s) {
+                         uint32_t* err, cudaStream_t s, Node2* records) {
     const SingleMesh seg{n};
     if (key_bytes == 4)
         return launch_t((const uint32_t*)keys, cluster_idx, parent, nodes, seg, 0u, n, radius, tokens,
-                        parent_of_last, leaf_ctr, err, 0u, s);
+                        parent_of_last, leaf_ctr, err, 0u, s, records);
     return launch_t((const uint64_t*)keys, cluster_idx, parent, nodes, seg, 0u, n, radius, tokens, parent_of_last,
-                    leaf_ctr, err, 0u, s);
+                    leaf_ctr, err, 0u, s, records);
 }
 
 cudaError_t launch_hploc_batch(const uint64_t* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,

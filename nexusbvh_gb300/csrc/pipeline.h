@@ -158,9 +158,11 @@ cudaError_t launch_sort63_hybrid(const uint64_t* keys_in, const uint32_t* vals_i
 // tokens: n words of scratch (no initialisation needed); parent_of_last:
 // one word that must hold INVALID on entry; leaf_ctr: one word that must
 // be zero on entry.
+// records: n records of 32 bytes (no initialisation needed), where merges
+// store each window's clusters as {box, id, token}.
 cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
                          uint32_t n, uint32_t radius, uint32_t* tokens, uint32_t* parent_of_last, uint32_t* leaf_ctr,
-                         uint32_t* err, cudaStream_t s);
+                         uint32_t* err, cudaStream_t s, Node2* records);
 // ---------------------------------------------------------------- stage 5
 // pairs: n uint64 slots; ctr: kBvh8CtrWords words (128-byte aligned).
 // Both are initialised by launch_bvh8_init.
