@@ -311,6 +311,154 @@ __global__ __launch_bounds__(kThreads, 4) void onesweep_kernel(const K* __restri
                                       s_local, s_tmp);
 }
 
+// The same pass for 32-bit keys (8-bit digits, one digit per thread) as a
+// kernel of its own: sort_tile compiled for 32-bit keys executes 24 % more
+// warp instructions (28.4 M against 22.8 M for a 4.19M-key pass) and takes
+// 11 % longer (0.478 against 0.428 ms for the four passes of 12.58M 30-bit
+// keys); for 64-bit keys sort_tile is not slower.
+template <bool HAS_VALS>
+__global__ __launch_bounds__(kThreads, 4) void onesweep32_kernel(const uint32_t* __restrict__ kin, uint32_t* __restrict__ kout,
+                                                            const uint32_t* __restrict__ vin,
+                                                            uint32_t* __restrict__ vout, uint32_t n, uint32_t shift,
+                                                            uint32_t bits, const uint32_t* __restrict__ hist,
+                                                            uint32_t* lookback, uint32_t* tile_ctr, uint32_t* err) {
+    using K = uint32_t;
+    constexpr int KPT = Tile<K>::kKeysPerThread;
+    constexpr int TILE = tile_keys<K>();
+    extern __shared__ __align__(16) unsigned char smem[];
+    K* s_keys = reinterpret_cast<K*>(smem);
+    uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
+    uint32_t* s_whist = s_vals + TILE;
+    __shared__ uint32_t s_local_start[kRadixBins];
+    __shared__ uint32_t s_global_start[kRadixBins];
+    __shared__ uint32_t s_tmp[kWarps];
+    __shared__ uint32_t s_tile;
+
+    const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
+    const uint32_t mask = (1u << bits) - 1u;
+    if (tid == 0) s_tile = atomicAdd(tile_ctr, 1u);
+    for (int i = tid; i < kWarps * kRadixBins; i += kThreads) s_whist[i] = 0;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t tile_base = tile * (uint32_t)TILE;
+    if (tile_base >= n) return;  // only reachable when a launch claims more tiles than exist
+    // global start of each digit (exclusive scan of this pass's histogram):
+    // only tile 0 needs it, the others inherit it through the look-back
+    uint32_t digit_base = 0;
+    if (tile == 0) digit_base = cta_exclusive_scan(tid <= mask ? hist[tid] : 0u, s_tmp);
+
+    // ---- load (warp-striped: warp w owns a contiguous run of 32*KPT keys)
+    K key[KPT];
+    uint32_t val[KPT];
+    uint32_t rank[KPT];
+    const uint32_t wbase = tile_base + warp * 32u * KPT + lane;
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+        const uint32_t idx = wbase + 32u * j;
+        const bool valid = idx < n;
+        key[j] = valid ? kin[idx] : (K)0;
+        if (HAS_VALS)
+            val[j] = valid ? vin[idx] : 0u;
+        else
+            val[j] = idx;
+    }
+
+    // ---- stable rank within the warp, one digit group at a time
+    uint32_t* wh = s_whist + warp * kRadixBins;
+    const uint32_t lt_mask = lanemask_lt();
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+        const bool valid = wbase + 32u * j < n;
+        const uint32_t d = (uint32_t)(key[j] >> shift) & mask;
+        uint32_t peers = __ballot_sync(kFullMask, valid);
+#pragma unroll
+        for (int b = 0; b < kRadixBits; ++b) {
+            if (b < (int)bits) {
+                const bool bit = (d >> b) & 1u;
+                const uint32_t bb = __ballot_sync(kFullMask, bit);
+                peers &= bit ? bb : ~bb;
+            }
+        }
+        const uint32_t below = __popc(peers & lt_mask);
+        const uint32_t leader = (uint32_t)(__ffs(peers) - 1) & 31u;
+        uint32_t base = 0;
+        if (valid && below == 0) {
+            base = wh[d];
+            wh[d] = base + __popc(peers);
+        }
+        base = __shfl_sync(kFullMask, base, leader);
+        rank[j] = base + below;
+        __syncwarp();
+    }
+    __syncthreads();
+
+    // ---- per-digit tile count and per-warp exclusive offsets (thread = digit)
+    uint32_t tile_cnt = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+        const uint32_t c = s_whist[w * kRadixBins + tid];
+        s_whist[w * kRadixBins + tid] = tile_cnt;
+        tile_cnt += c;
+    }
+
+    // ---- publish, then decoupled look-back for this digit
+    uint32_t* lb = lookback + (size_t)tile * kRadixBins;
+    uint32_t excl = 0;
+    if (tid <= mask) {
+        if (tile == 0) {
+            excl = digit_base;
+            atomicExch(lb + tid, kFlagInc | (excl + tile_cnt));
+        } else {
+            atomicExch(lb + tid, kFlagAgg | tile_cnt);
+            int32_t pred = (int32_t)tile - 1;
+            uint32_t polls = 0;
+            while (pred >= 0) {
+                const uint32_t v = ld_relaxed_u32(lookback + (size_t)pred * kRadixBins + tid);
+                const uint32_t flag = v & ~kCountMask;
+                if (flag == 0) {
+                    if (++polls > kSpinLimit) {
+                        set_error(err, NXB_DEVERR_SORT_LOOKBACK_TIMEOUT);
+                        break;
+                    }
+                    if (polls > 64) __nanosleep(64);
+                    continue;
+                }
+                excl += v & kCountMask;
+                if (flag == kFlagInc) break;
+                --pred;
+            }
+            atomicExch(lb + tid, kFlagInc | (excl + tile_cnt));
+        }
+    }
+    s_global_start[tid] = excl;
+    s_local_start[tid] = cta_exclusive_scan(tid <= mask ? tile_cnt : 0u, s_tmp);
+    __syncthreads();
+
+    // ---- reorder the tile by digit in shared memory
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+        if (wbase + 32u * j < n) {
+            const uint32_t d = (uint32_t)(key[j] >> shift) & mask;
+            const uint32_t pos = s_local_start[d] + wh[d] + rank[j];
+            s_keys[pos] = key[j];
+            s_vals[pos] = val[j];
+        }
+    }
+    __syncthreads();
+
+    // ---- scatter runs of equal digits to consecutive global addresses
+    const uint32_t tile_n = min((uint32_t)TILE, n - tile_base);
+    for (uint32_t i = tid; i < tile_n; i += kThreads) {
+        const K k = s_keys[i];
+        const uint32_t d = (uint32_t)(k >> shift) & mask;
+        const uint32_t g = s_global_start[d] + (i - s_local_start[d]);
+        if (g < n) {  // always true unless a look-back wait expired
+            kout[g] = k;
+            vout[g] = s_vals[i];
+        }
+    }
+}
+
 // Dynamic shared memory above the 48 KB default (the 9-bit tables) and the
 // carveout for four tiles per SM: shared memory, not L1.
 template <typename Kern>
@@ -324,8 +472,14 @@ template <typename K, int RB>
 cudaError_t configure_onesweep() {
     return once_per_device([] {
         constexpr size_t smem = dyn_smem_bytes<K, RB>();
-        cudaError_t r = set_smem_attributes(onesweep_kernel<K, true, RB>, smem);
-        if (!r) r = set_smem_attributes(onesweep_kernel<K, false, RB>, smem);
+        cudaError_t r;
+        if constexpr (sizeof(K) == 4) {
+            r = set_smem_attributes(onesweep32_kernel<true>, smem);
+            if (!r) r = set_smem_attributes(onesweep32_kernel<false>, smem);
+        } else {
+            r = set_smem_attributes(onesweep_kernel<K, true, RB>, smem);
+            if (!r) r = set_smem_attributes(onesweep_kernel<K, false, RB>, smem);
+        }
         return r;
     });
 }
@@ -338,12 +492,22 @@ cudaError_t launch_pass_t(const K* kin, K* kout, const uint32_t* vin, uint32_t* 
     cudaError_t e = configure_onesweep<K, RB>();
     if (e != cudaSuccess) return e;
     const uint32_t tiles = (n + tile_keys<K>() - 1) / tile_keys<K>();
-    if (vin)
-        onesweep_kernel<K, true, RB><<<tiles, kThreads, smem, s>>>(kin, kout, vin, vout, n, shift, bits, hist,
-                                                                  lookback, tile_ctr, err);
-    else
-        onesweep_kernel<K, false, RB><<<tiles, kThreads, smem, s>>>(kin, kout, vin, vout, n, shift, bits, hist,
+    if constexpr (sizeof(K) == 4) {
+        static_assert(RB == kRadixBits, "32-bit keys take 8-bit digits");
+        if (vin)
+            onesweep32_kernel<true><<<tiles, kThreads, smem, s>>>(kin, kout, vin, vout, n, shift, bits, hist, lookback,
+                                                                  tile_ctr, err);
+        else
+            onesweep32_kernel<false><<<tiles, kThreads, smem, s>>>(kin, kout, vin, vout, n, shift, bits, hist,
                                                                    lookback, tile_ctr, err);
+    } else {
+        if (vin)
+            onesweep_kernel<K, true, RB><<<tiles, kThreads, smem, s>>>(kin, kout, vin, vout, n, shift, bits, hist,
+                                                                      lookback, tile_ctr, err);
+        else
+            onesweep_kernel<K, false, RB><<<tiles, kThreads, smem, s>>>(kin, kout, vin, vout, n, shift, bits, hist,
+                                                                       lookback, tile_ctr, err);
+    }
     return cudaGetLastError();
 }
 
@@ -649,8 +813,7 @@ cudaError_t run_sort_stall_probe(uint32_t* err_out) {
     constexpr size_t smem = dyn_smem_bytes<uint32_t, kRadixBits>();
     if (!e) e = configure_onesweep<uint32_t, kRadixBits>();
     if (!e) {
-        onesweep_kernel<uint32_t, false, kRadixBits><<<1, kThreads, smem>>>(keys, kout, nullptr, vout, n, 0, 8, hist,
-                                                                            lookback, ctr, err);
+        onesweep32_kernel<false><<<1, kThreads, smem>>>(keys, kout, nullptr, vout, n, 0, 8, hist, lookback, ctr, err);
         e = cudaGetLastError();
     }
     if (!e) e = cudaMemcpy(err_out, err, 4, cudaMemcpyDeviceToHost);
