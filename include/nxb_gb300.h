@@ -297,9 +297,10 @@ nxb_status nxb_stage_radix_sort_noalloc(uint32_t key_bytes, const void* d_keys_i
                                         struct CUstream_st* stream);
 
 /* Stage 4 (BuildBVH2Kernel): H-PLOC over sorted keys; d_cluster_idx is the
- * sorted permutation (it is overwritten); d_nodes leaves [0,n) must hold the
- * stage-1 output; internal nodes are written to [n, 2n-1).  Scratch:
- * nxb_hploc_scratch_bytes(). */
+ * sorted permutation (treat its contents as undefined afterwards); d_nodes
+ * leaves [0,n) must hold the stage-1 output; internal nodes are written to
+ * [n, 2n-1).  Scratch: nxb_hploc_scratch_bytes() (about 40 bytes per
+ * primitive: hand-over slots, tokens and 32-byte cluster records). */
 size_t nxb_hploc_scratch_bytes(uint32_t prim_count);
 nxb_status nxb_stage_hploc(uint32_t key_bytes, const void* d_sorted_keys,
                            uint32_t* d_cluster_idx, nxb_bvh2_node* d_nodes,
