@@ -57,11 +57,35 @@ __device__ __forceinline__ uint64_t delta(const MeshKey* k, uint32_t a, uint32_t
     return (((uint64_t)ka << 32) | (a - s)) ^ (((uint64_t)kb << 32) | (b - s));
 }
 
+// The warp's row of shared memory: cluster k of the window at row[k]
+// (min xyz, max x) and row[32 + k] (max yz, id, token).
+__device__ __forceinline__ void put_row(uint4* row, uint32_t k, const Box& b, uint32_t cid, uint32_t ctok) {
+    row[k] = make_uint4(__float_as_uint(b.mn.x), __float_as_uint(b.mn.y), __float_as_uint(b.mn.z),
+                        __float_as_uint(b.mx.x));
+    row[32 + k] = make_uint4(__float_as_uint(b.mx.y), __float_as_uint(b.mx.z), cid, ctok);
+}
+__device__ __forceinline__ Box row_box(const uint4* row, uint32_t k) {
+    const uint4 a = row[k];
+    const uint2 b = *reinterpret_cast<const uint2*>(row + 32 + k);
+    Box r;
+    r.mn = make_float3(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z));
+    r.mx = make_float3(__uint_as_float(a.w), __uint_as_float(b.x), __uint_as_float(b.y));
+    return r;
+}
+
 // COVER selects the difference-cover search (single-mesh builds, where it
 // measured faster at every radius; the batched kernel keeps the plain one).
-template <int R, bool COVER>
-__device__ __forceinline__ uint32_t nearest_neighbour(uint32_t num, const Box& cb) {
+// ROW: the neighbour boxes are read from the warp's row of shared memory
+// instead of shuffled (see merge_step).
+template <int R, bool COVER, bool ROW = false>
+__device__ __forceinline__ uint32_t nearest_neighbour(uint32_t num, const Box& cb, const uint4* row = nullptr) {
     const uint32_t lane = lane_id();
+    auto fetch = [&](uint32_t k) -> Box {
+        if constexpr (ROW)
+            return row_box(row, (lane + k) & 31u);
+        else
+            return shfl_box(cb, (lane + k) & 31u);
+    };
     uint32_t best = kInvalid, best_idx = kInvalid;
     if constexpr (R == 4 && COVER) {
         // marks {0, 1, 2, 4}: 1 = 1-0, 2 = 2-0, 3 = 4-1, 4 = 4-0
@@ -83,13 +107,13 @@ __device__ __forceinline__ uint32_t nearest_neighbour(uint32_t num, const Box& c
                 best_idx = lane - d;
             }
         };
-        const Box b1 = shfl_box(cb, (lane + 1) & 31u);
+        const Box b1 = fetch(1);
         pick(pair(cb, b1, 0, 1), 0, 1);
         {
-            const Box b2 = shfl_box(cb, (lane + 2) & 31u);
+            const Box b2 = fetch(2);
             pick(pair(cb, b2, 0, 2), 0, 2);
         }
-        const Box b4 = shfl_box(cb, (lane + 4) & 31u);
+        const Box b4 = fetch(4);
         const uint32_t f3 = pair(b1, b4, 1, 3), f4 = pair(cb, b4, 0, 4);
         pick(f3, 1, 3);
         pick(f4, 0, 4);
@@ -123,19 +147,19 @@ __device__ __forceinline__ uint32_t nearest_neighbour(uint32_t num, const Box& c
                 best_idx = lane - d;
             }
         };
-        const Box b1 = shfl_box(cb, (lane + 1) & 31u);
-        const Box b2 = shfl_box(cb, (lane + 2) & 31u);
+        const Box b1 = fetch(1);
+        const Box b2 = fetch(2);
         pick(pair(cb, b1, 0, 1), 0, 1);
         pick(pair(cb, b2, 0, 2), 0, 2);
         {
-            const Box b5 = shfl_box(cb, (lane + 5) & 31u);
+            const Box b5 = fetch(5);
             const uint32_t f3 = pair(b2, b5, 2, 3), f4 = pair(b1, b5, 1, 4), f5 = pair(cb, b5, 0, 5);
             pick(f3, 2, 3);
             pick(f4, 1, 4);
             pick(f5, 0, 5);
         }
         {
-            const Box b8 = shfl_box(cb, (lane + 8) & 31u);
+            const Box b8 = fetch(8);
             const uint32_t f6 = pair(b2, b8, 2, 6), f7 = pair(b1, b8, 1, 7), f8 = pair(cb, b8, 0, 8);
             pick(f6, 2, 6);
             pick(f7, 1, 7);
@@ -145,21 +169,21 @@ __device__ __forceinline__ uint32_t nearest_neighbour(uint32_t num, const Box& c
             // distances 9..16 are 8 + (1..8): the same low boxes 0, 1, 2
             // against the boxes of lanes +9, +10, +13 and +16
             {
-                const Box b9 = shfl_box(cb, (lane + 9) & 31u);
+                const Box b9 = fetch(9);
                 pick(pair(cb, b9, 0, 9), 0, 9);
             }
             {
-                const Box b10 = shfl_box(cb, (lane + 10) & 31u);
+                const Box b10 = fetch(10);
                 pick(pair(cb, b10, 0, 10), 0, 10);
             }
             {
-                const Box b13 = shfl_box(cb, (lane + 13) & 31u);
+                const Box b13 = fetch(13);
                 const uint32_t f11 = pair(b2, b13, 2, 11), f12 = pair(b1, b13, 1, 12), f13 = pair(cb, b13, 0, 13);
                 pick(f11, 2, 11);
                 pick(f12, 1, 12);
                 pick(f13, 0, 13);
             }
-            const Box b16 = shfl_box(cb, (lane + 16) & 31u);
+            const Box b16 = fetch(16);
             const uint32_t f14 = pair(b2, b16, 2, 14), f15 = pair(b1, b16, 1, 15), f16 = pair(cb, b16, 0, 16);
             pick(f14, 2, 14);
             pick(f15, 1, 15);
@@ -205,17 +229,34 @@ struct MergeCtx {
 // absorb the tokens 1..n-1 exactly once, and node n-1+token(j) is a
 // collision-free index in [n, 2n-1) that needs no global counter (the
 // reference takes one atomicAdd on a single counter per merge round).
+// ROW: the window's clusters also live in the warp's row of shared memory,
+// which holds them at the start of every round: the merge reads its
+// partner there, and the order-preserving compaction goes through it (each
+// kept cluster written at its rank, every lane reading its own slot)
+// instead of a find-n-th-set-bit and eight shuffles.
+template <bool ROW>
 __device__ __forceinline__ uint32_t merge_step(const MergeCtx& m, uint32_t num, uint32_t nn, uint32_t& cid,
-                                               uint32_t& ctok, Box& cb) {
+                                               uint32_t& ctok, Box& cb, uint4* row) {
     const uint32_t lane = lane_id();
     const uint32_t nn_of_nn = __shfl_sync(kFullMask, nn, nn & 31u);
     const bool mutual = lane < num && lane == nn_of_nn;
     const bool merge = mutual && lane < nn;
     const uint32_t mmask = __ballot_sync(kFullMask, merge);
     const uint32_t mcount = __popc(mmask);
-    const uint32_t ncid = __shfl_sync(kFullMask, cid, nn & 31u);
-    const uint32_t ntok = __shfl_sync(kFullMask, ctok, nn & 31u);
-    const Box nb = shfl_box(cb, nn & 31u);
+    uint32_t ncid, ntok;
+    Box nb;
+    if constexpr (ROW) {
+        if (merge) {
+            nb = row_box(row, nn & 31u);
+            const uint2 it = *reinterpret_cast<const uint2*>(&row[32 + (nn & 31u)].z);
+            ncid = it.x;
+            ntok = it.y;
+        }
+    } else {
+        ncid = __shfl_sync(kFullMask, cid, nn & 31u);
+        ntok = __shfl_sync(kFullMask, ctok, nn & 31u);
+        nb = shfl_box(cb, nn & 31u);
+    }
     if (merge) {
         grow(cb, nb);
         const uint32_t idx = m.n - 1 + ntok;
@@ -228,11 +269,27 @@ __device__ __forceinline__ uint32_t merge_step(const MergeCtx& m, uint32_t num, 
         cid = idx;
     }
     const uint32_t vmask = __ballot_sync(kFullMask, merge || !mutual);
-    const int sh = __fns(vmask, 0, lane + 1);
-    cid = __shfl_sync(kFullMask, cid, (uint32_t)sh & 31u);
-    ctok = __shfl_sync(kFullMask, ctok, (uint32_t)sh & 31u);
-    cb = shfl_box(cb, (uint32_t)sh & 31u);
-    if (sh < 0) cid = kInvalid;
+    if constexpr (ROW) {
+        const uint32_t rank = __popc(vmask & lanemask_lt());
+        __syncwarp();  // the previous round's reads of the row are done
+        if ((vmask >> lane) & 1u) put_row(row, rank, cb, cid, ctok);
+        __syncwarp();
+        if (lane < (uint32_t)__popc(vmask)) {
+            const uint4 a = row[lane], b = row[32 + lane];
+            cb.mn = make_float3(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z));
+            cb.mx = make_float3(__uint_as_float(a.w), __uint_as_float(b.x), __uint_as_float(b.y));
+            cid = b.z;
+            ctok = b.w;
+        } else {
+            cid = kInvalid;
+        }
+    } else {
+        const int sh = __fns(vmask, 0, lane + 1);
+        cid = __shfl_sync(kFullMask, cid, (uint32_t)sh & 31u);
+        ctok = __shfl_sync(kFullMask, ctok, (uint32_t)sh & 31u);
+        cb = shfl_box(cb, (uint32_t)sh & 31u);
+        if (sh < 0) cid = kInvalid;
+    }
     return num - mcount;
 }
 
@@ -306,7 +363,8 @@ __device__ __forceinline__ MergeCtx mesh_ctx(const MergeCtx& all, const Seg& seg
 // addresses that mesh's nodes.
 template <int R, bool COVER, bool REC>
 __device__ __forceinline__ void merge_windows(uint32_t owner, uint32_t left, uint32_t right, uint32_t split,
-                                              bool final, uint32_t start, uint32_t* cluster, const MergeCtx& m) {
+                                              bool final, uint32_t start, uint32_t* cluster, const MergeCtx& m,
+                                              uint4* row) {
     const uint32_t lane = lane_id();
     const uint32_t l_start = __shfl_sync(kFullMask, left, owner);
     const uint32_t r_end = __shfl_sync(kFullMask, right, owner) + 1;
@@ -382,6 +440,10 @@ __device__ __forceinline__ void merge_windows(uint32_t owner, uint32_t left, uin
             cb.mx = cb.mn;
         }
     }
+    if constexpr (REC) {
+        put_row(row, lane, cb, cid, ctok);
+        __syncwarp();
+    }
     const uint32_t threshold = fin ? 1u : kMergeThreshold;
     while (num > threshold) {
         if (fin && num == 2) {
@@ -389,8 +451,8 @@ __device__ __forceinline__ void merge_windows(uint32_t owner, uint32_t left, uin
             num = 1;
             break;
         }
-        const uint32_t nn = nearest_neighbour<R, COVER>(num, cb);
-        num = merge_step(m, num, nn, cid, ctok, cb);
+        const uint32_t nn = nearest_neighbour<R, COVER, REC>(num, cb, row);
+        num = merge_step<REC>(m, num, nn, cid, ctok, cb, row);
     }
     // StoreIndices (BinaryBuilder.cu:59-69)
     if (lane < num_left + num_right) {
@@ -411,13 +473,14 @@ __device__ __forceinline__ void merge_windows(uint32_t owner, uint32_t left, uin
 // launch bounds above neither kernel spills).
 template <int R, typename Seg>
 __device__ __forceinline__ void ploc_merge(uint32_t owner, uint32_t left, uint32_t right, uint32_t split, bool final,
-                                        MeshSpan me, uint32_t* cluster, const MergeCtx& all, const Seg& seg) {
+                                        MeshSpan me, uint32_t* cluster, const MergeCtx& all, const Seg& seg,
+                                        uint4* row) {
     if constexpr (Seg::kBatch) {
         uint32_t start;
         const MergeCtx m = mesh_ctx<Seg>(all, seg, me, owner, start);
-        merge_windows<R, false, false>(owner, left, right, split, final, start, cluster, m);
+        merge_windows<R, false, false>(owner, left, right, split, final, start, cluster, m, row);
     } else {
-        merge_windows<R, true, true>(owner, left, right, split, final, 0u, cluster, all);
+        merge_windows<R, true, true>(owner, left, right, split, final, 0u, cluster, all, row);
     }
 }
 
@@ -464,6 +527,9 @@ __global__ __launch_bounds__(kThreads, hploc_ctas_per_sm<R, Seg>()) void hploc_k
                                                          uint32_t* err, uint32_t end, uint32_t chunk, Node2* rec) {
     const uint32_t lane = lane_id();
     const MergeCtx all{nodes, tok, rec, parent_of_last, end, 2 * end - 1, err};
+    // each warp's row for the merge compaction (single-mesh builds)
+    __shared__ uint4 s_rows[Seg::kBatch ? 1 : kThreads / 32][64];
+    uint4* row = s_rows[Seg::kBatch ? 0 : threadIdx.x >> 5];
     uint32_t left = 0, right = 0, split = 0;
     // the lane's mesh; a plain build has one, known at compile time
     MeshSpan me = Seg::kBatch ? MeshSpan{0, 0, 0} : seg.of_prim(0);
@@ -526,7 +592,7 @@ __global__ __launch_bounds__(kThreads, hploc_ctas_per_sm<R, Seg>()) void hploc_k
             fence_acq_rel_gpu();  // acquire: the siblings' clusters
             while (todo) {
                 const uint32_t owner = __ffs(todo) - 1;
-                ploc_merge<R, Seg>(owner, left, right, split, final, me, cluster, all, seg);
+                ploc_merge<R, Seg>(owner, left, right, split, final, me, cluster, all, seg, row);
                 todo &= todo - 1;
             }
             __syncwarp();
