@@ -197,10 +197,11 @@ nxb_status enqueue_build(const void* prims, nxb_prim_type type, uint32_t n, cons
     // the sort's second value buffer holds the H-PLOC cluster tokens
     NXB_TRY(launch_hploc(L.key_bytes, keys_a, vals_a, parent, bvh2, n, radius_of(cfg), vals_b,
                          &ctrl->parent_of_last, &ctrl->hploc_leaf_ctr, &ctrl->error_word, s,
-                         reinterpret_cast<Node2*>(ws + L.records)));
+                         reinterpret_cast<Node2*>(ws + L.records), bvh8 ? pairs : nullptr,
+                         bvh8 ? ctrl->bvh8_ctr : nullptr));
     NXB_TRY(mark(4));
     if (bvh8) {
-        NXB_TRY(launch_bvh8_init(pairs, n, ctrl->bvh8_ctr, s));
+        // the climb initialised the collapse's work queue
         NXB_TRY(launch_bvh8(bvh2, n, bvh8, (uint32_t)bvh8_capacity(n), prim_idx, pairs, ctrl->bvh8_ctr,
                             &ctrl->error_word, auction_of(cfg), s));
     }

@@ -524,8 +524,10 @@ template <typename K, int R, typename Seg>
 __global__ __launch_bounds__(kThreads, hploc_ctas_per_sm<R, Seg>()) void hploc_kernel(const K* __restrict__ keys, uint32_t* cluster,
                                                          uint32_t* parent, Node2* nodes, Seg seg, uint32_t begin,
                                                          uint32_t* tok, uint32_t* parent_of_last, uint32_t* leaf_ctr,
-                                                         uint32_t* err, uint32_t end, uint32_t chunk, Node2* rec) {
+                                                         uint32_t* err, uint32_t end, uint32_t chunk, Node2* rec,
+                                                         uint64_t* bvh8_pairs, uint32_t* bvh8_ctr) {
     const uint32_t lane = lane_id();
+    if (!Seg::kBatch && bvh8_ctr && blockIdx.x == 0 && threadIdx.x == 0) bvh8_queue_counters(bvh8_ctr);
     const MergeCtx all{nodes, tok, rec, parent_of_last, end, 2 * end - 1, err};
     // each warp's row for the merge compaction (single-mesh builds)
     __shared__ uint4 s_rows[Seg::kBatch ? 1 : kThreads / 32][64];
@@ -556,7 +558,11 @@ __global__ __launch_bounds__(kThreads, hploc_ctas_per_sm<R, Seg>()) void hploc_k
             if (!active && ((need >> lane) & 1u) && rank < avail) {
                 left = right = chunk_next + rank;
                 active = true;
-                if constexpr (Seg::kBatch) me = seg.of_prim(left);
+                if constexpr (Seg::kBatch) {
+                    me = seg.of_prim(left);
+                } else if (bvh8_pairs) {
+                    bvh8_pairs[left] = bvh8_queue_slot(left, end);
+                }
             }
             const uint32_t took = min((uint32_t)__popc(need), avail);
             chunk_next += took;
@@ -604,7 +610,7 @@ __global__ __launch_bounds__(kThreads, hploc_ctas_per_sm<R, Seg>()) void hploc_k
 template <typename K, int R, typename Seg>
 cudaError_t launch_r(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, Seg seg, uint32_t begin,
                      uint32_t end, uint32_t* tok, uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err,
-                     uint32_t max_per_sm, cudaStream_t s, Node2* rec) {
+                     uint32_t max_per_sm, cudaStream_t s, Node2* rec, uint64_t* pairs, uint32_t* ctr) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hploc_kernel<K, R, Seg>, kThreads, 0);
     if (max_per_sm && (uint32_t)per_sm > max_per_sm) per_sm = (int)max_per_sm;
@@ -613,24 +619,25 @@ cudaError_t launch_r(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* 
     const uint32_t grid = std::max(1u, std::min(want, (uint32_t)(device_info().sms * per_sm)));
     const uint32_t chunk = leaf_chunk(end - begin, grid * (kThreads / 32), Seg::kBatch);
     hploc_kernel<K, R, Seg><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, seg, begin, tok, pol, leaf_ctr,
-                                                      err, end, chunk, rec);
+                                                      err, end, chunk, rec, pairs, ctr);
     return cudaGetLastError();
 }
 
 template <typename K, typename Seg>
 cudaError_t launch_t(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, Seg seg, uint32_t begin,
                      uint32_t end, uint32_t radius, uint32_t* tok, uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err,
-                     uint32_t max_per_sm, cudaStream_t s, Node2* rec = nullptr) {
+                     uint32_t max_per_sm, cudaStream_t s, Node2* rec = nullptr, uint64_t* pairs = nullptr,
+                     uint32_t* ctr = nullptr) {
     switch (radius) {
         case 4:
             return launch_r<K, 4>(keys, cluster, parent, nodes, seg, begin, end, tok, pol, leaf_ctr, err, max_per_sm,
-                                  s, rec);
+                                  s, rec, pairs, ctr);
         case 16:
             return launch_r<K, 16>(keys, cluster, parent, nodes, seg, begin, end, tok, pol, leaf_ctr, err,
-                                   max_per_sm, s, rec);
+                                   max_per_sm, s, rec, pairs, ctr);
         default:
             return launch_r<K, 8>(keys, cluster, parent, nodes, seg, begin, end, tok, pol, leaf_ctr, err, max_per_sm,
-                                  s, rec);
+                                  s, rec, pairs, ctr);
     }
 }
 
@@ -638,13 +645,14 @@ cudaError_t launch_t(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* 
 
 cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
                          uint32_t n, uint32_t radius, uint32_t* tokens, uint32_t* parent_of_last, uint32_t* leaf_ctr,
-                         uint32_t* err, cudaStream_t s, Node2* records) {
+                         uint32_t* err, cudaStream_t s, Node2* records, uint64_t* bvh8_pairs, uint32_t* bvh8_ctr) {
     const SingleMesh seg{n};
+    if (!bvh8_pairs != !bvh8_ctr) return cudaErrorInvalidValue;
     if (key_bytes == 4)
         return launch_t((const uint32_t*)keys, cluster_idx, parent, nodes, seg, 0u, n, radius, tokens,
-                        parent_of_last, leaf_ctr, err, 0u, s, records);
+                        parent_of_last, leaf_ctr, err, 0u, s, records, bvh8_pairs, bvh8_ctr);
     return launch_t((const uint64_t*)keys, cluster_idx, parent, nodes, seg, 0u, n, radius, tokens, parent_of_last,
-                    leaf_ctr, err, 0u, s, records);
+                    leaf_ctr, err, 0u, s, records, bvh8_pairs, bvh8_ctr);
 }
 
 cudaError_t launch_hploc_batch(const uint64_t* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,

@@ -21,6 +21,20 @@ constexpr int kMaxSortPasses = 10;
 // slots allocated, work items allocated but not finished.
 constexpr int kBvh8Claim = 0, kBvh8Nodes = 32, kBvh8Leaves = 64, kBvh8Alloc = 96, kBvh8Pending = 128;
 constexpr int kBvh8CtrWords = 160;
+
+// The BVH8 work queue of an n-primitive build before the collapse: slot 0
+// holds the root item (BVH2 root 2n-2 into BVH8 node 0), every other slot
+// is empty; one BVH8 node and one work item exist.
+__device__ __forceinline__ uint64_t bvh8_queue_slot(uint32_t i, uint32_t n) {
+    return i == 0 ? ((uint64_t)(2 * n - 2) << 32) : ~0ull;
+}
+__device__ __forceinline__ void bvh8_queue_counters(uint32_t* ctr) {
+    ctr[kBvh8Claim] = 0;
+    ctr[kBvh8Nodes] = 1;
+    ctr[kBvh8Leaves] = 0;
+    ctr[kBvh8Alloc] = 1;
+    ctr[kBvh8Pending] = 1;
+}
 constexpr int kRadixBits = 8;
 constexpr int kRadixBins = 1 << kRadixBits;
 // Widest digit of a onesweep pass (the pipeline's 63-bit sort uses 9-bit
@@ -160,9 +174,14 @@ cudaError_t launch_sort63_hybrid(const uint64_t* keys_in, const uint32_t* vals_i
 // be zero on entry.
 // records: n records of 32 bytes (no initialisation needed), where merges
 // store each window's clusters as {box, id, token}.
+// bvh8_pairs / bvh8_ctr (both or neither): the BVH8 work queue of stage 5,
+// which the climb initialises as launch_bvh8_init would (each lane writes
+// the slot of the leaf it takes), so that the collapse can follow without
+// an initialisation launch of its own.
 cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
                          uint32_t n, uint32_t radius, uint32_t* tokens, uint32_t* parent_of_last, uint32_t* leaf_ctr,
-                         uint32_t* err, cudaStream_t s, Node2* records);
+                         uint32_t* err, cudaStream_t s, Node2* records, uint64_t* bvh8_pairs = nullptr,
+                         uint32_t* bvh8_ctr = nullptr);
 // ---------------------------------------------------------------- stage 5
 // pairs: n uint64 slots; ctr: kBvh8CtrWords words (128-byte aligned).
 // Both are initialised by launch_bvh8_init.

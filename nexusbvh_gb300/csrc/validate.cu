@@ -100,8 +100,15 @@ __device__ __forceinline__ void report_max(uint64_t* w, uint32_t v) {
 // One round: link[i] = link[link[i].ancestor] composed with link[i].  The
 // root and unlinked nodes are terminal.  Words are read and written in
 // place: a word read in the same round is at least as far along as the
-// round-start value, so the rounds only converge faster.
-__global__ __launch_bounds__(kThreads) void jump_kernel(uint64_t* link, uint32_t count, uint32_t root) {
+// round-start value, so the rounds only converge faster.  A round that
+// changes no word leaves a fixed point, so every later round would change
+// none either: round r sets moved[r] when it changed a word, and round r+1
+// returns at once when moved[r] is clear (the rounds of a tree of depth D
+// stop after about log2(D) of them instead of log2(nodes)).
+__global__ __launch_bounds__(kThreads) void jump_kernel(uint64_t* link, uint32_t count, uint32_t root,
+                                                        const uint32_t* prev_moved, uint32_t* moved) {
+    if (prev_moved && *prev_moved == 0) return;
+    bool changed = false;
     for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < count; i += gridDim.x * kThreads) {
         if (i == root) continue;
         const uint64_t x = ld_relaxed_u64(link + i);
@@ -109,8 +116,13 @@ __global__ __launch_bounds__(kThreads) void jump_kernel(uint64_t* link, uint32_t
         if (a == root || a >= count) continue;
         const uint64_t y = ld_relaxed_u64(link + a);
         const uint64_t d = min((uint64_t)link_dist(x) + link_dist(y), (uint64_t)0xFFFFFFFEu);
-        st_relaxed_u64(link + i, pack_link(link_node(y), (uint32_t)d));
+        const uint64_t next = pack_link(link_node(y), (uint32_t)d);
+        if (next != x) {
+            st_relaxed_u64(link + i, next);
+            changed = true;
+        }
     }
+    if (__syncthreads_or(changed) && threadIdx.x == 0) *moved = 1;
 }
 
 // Parent references: [i] = extra references of node i (all of them for the
@@ -358,17 +370,26 @@ uint32_t jump_rounds(uint32_t count) {
     return r;
 }
 
+// The rounds of pointer jumping, each skipped once a round before it moved
+// no link; moved holds one word per round.
+void jump(uint64_t* link, uint32_t count, uint32_t root, uint32_t* moved, uint32_t grid, cudaStream_t s) {
+    for (uint32_t r = 0, rounds = jump_rounds(count); r < rounds; ++r)
+        jump_kernel<<<grid, kThreads, 0, s>>>(link, count, root, r ? moved + r - 1 : nullptr, moved + r);
+}
+
+constexpr size_t kMovedBytes = 4 * 32;
+
 size_t seg(size_t bytes) { return (bytes + 255) / 256 * 256; }
 
 }  // namespace
 
 size_t validate_bvh2_scratch(uint32_t n) {
     const size_t total = 2ull * n - 1;
-    return seg(8 * total) + seg(4 * total) + seg(4ull * n);
+    return seg(8 * total) + seg(4 * total) + seg(4ull * n) + seg(kMovedBytes);
 }
 
 size_t validate_bvh8_scratch(uint32_t m, uint32_t n) {
-    return seg(8ull * m) + 3 * seg(4ull * m) + seg(24ull * m) + seg(4ull * n);
+    return seg(8ull * m) + 3 * seg(4ull * m) + seg(24ull * m) + seg(4ull * n) + seg(kMovedBytes);
 }
 
 cudaError_t launch_validate_bvh2(const Node2* nodes, uint32_t n, uint32_t root, uint64_t* report, void* scratch,
@@ -380,15 +401,17 @@ cudaError_t launch_validate_bvh2(const Node2* nodes, uint32_t n, uint32_t root, 
     uint32_t* pcount = reinterpret_cast<uint32_t*>(p);
     p += seg(4ull * total);
     uint32_t* seen = reinterpret_cast<uint32_t*>(p);
+    p += seg(4ull * n);
+    uint32_t* moved = reinterpret_cast<uint32_t*>(p);
     cudaError_t e = cudaMemsetAsync(report, 0, NXB_BVH2_CHECK_FIELDS * sizeof(uint64_t), s);
     if (!e) e = cudaMemsetAsync(link, 0xFF, 8ull * total, s);
     if (!e) e = cudaMemsetAsync(pcount, 0, 4ull * total, s);
     if (!e) e = cudaMemsetAsync(seen, 0, 4ull * n, s);
+    if (!e) e = cudaMemsetAsync(moved, 0, kMovedBytes, s);
     if (e) return e;
     const uint32_t g = grid_for(total);
     bvh2_link_kernel<<<g, kThreads, 0, s>>>(nodes, total, link, pcount);
-    for (uint32_t r = 0, rounds = jump_rounds(total); r < rounds; ++r)
-        jump_kernel<<<g, kThreads, 0, s>>>(link, total, root);
+    jump(link, total, root, moved, g, s);
     bvh2_check_kernel<<<g, kThreads, 0, s>>>(nodes, n, root, link, pcount, seen, report);
     prim_count_kernel<<<grid_for(n), kThreads, 0, s>>>(seen, n, report + 2, report + 3);
     bvh2_errors_kernel<<<1, 32, 0, s>>>(report, n);
@@ -410,17 +433,20 @@ cudaError_t launch_validate_bvh8(const Node8* nodes, uint32_t m, const uint32_t*
     w.sub = reinterpret_cast<float*>(p);
     p += seg(24ull * m);
     w.seen = reinterpret_cast<uint32_t*>(p);
+    p += seg(4ull * n);
+    uint32_t* moved = reinterpret_cast<uint32_t*>(p);
     cudaError_t e = cudaMemsetAsync(report, 0, NXB_BVH8_CHECK_FIELDS * sizeof(uint64_t), s);
     if (!e) e = cudaMemsetAsync(w.link, 0xFF, 8ull * m, s);
     if (!e) e = cudaMemsetAsync(w.par, 0xFF, 4ull * m, s);
     if (!e) e = cudaMemsetAsync(w.pcount, 0, 4ull * m, s);
     if (!e) e = cudaMemsetAsync(w.seen, 0, 4ull * n, s);
+    if (!e) e = cudaMemsetAsync(moved, 0, kMovedBytes, s);
     if (e) return e;
     const float* f = static_cast<const float*>(prims);
     const uint32_t g = grid_for(m);
     bvh8_link_kernel<<<g, kThreads, 0, s>>>(nodes, m, w);
     bvh8_box_kernel<<<g, kThreads, 0, s>>>(nodes, m, prim_idx, n, f, prim_type, w);
-    for (uint32_t r = 0, rounds = jump_rounds(m); r < rounds; ++r) jump_kernel<<<g, kThreads, 0, s>>>(w.link, m, 0);
+    jump(w.link, m, 0, moved, g, s);
     bvh8_check_kernel<<<g, kThreads, 0, s>>>(nodes, m, prim_idx, n, f, prim_type, w, report);
     prim_count_kernel<<<grid_for(n), kThreads, 0, s>>>(w.seen, n, report + 2, report + 3);
     bvh8_errors_kernel<<<1, 32, 0, s>>>(report, m, n);

@@ -251,15 +251,8 @@ struct LeafZero {
 
 __global__ void bvh8_init_kernel(uint64_t* pairs, uint32_t n, uint32_t* ctr) {
     const uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x;
-    for (uint32_t i = i0; i < n; i += gridDim.x * blockDim.x)
-        pairs[i] = i == 0 ? ((uint64_t)(2 * n - 2) << 32) : ~0ull;
-    if (i0 == 0) {
-        ctr[kBvh8Claim] = 0;    // next work slot to claim
-        ctr[kBvh8Nodes] = 1;    // BVH8 nodes allocated (the root)
-        ctr[kBvh8Leaves] = 0;   // leaves allocated
-        ctr[kBvh8Alloc] = 1;    // work slots allocated (the root's)
-        ctr[kBvh8Pending] = 1;  // work items allocated but not finished
-    }
+    for (uint32_t i = i0; i < n; i += gridDim.x * blockDim.x) pairs[i] = bvh8_queue_slot(i, n);
+    if (i0 == 0) bvh8_queue_counters(ctr);
 }
 
 // Batched form: slot m holds the root item of mesh m (empty meshes too,
