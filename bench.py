@@ -153,11 +153,12 @@ def make_prims(name: str) -> np.ndarray:
 
 
 def cpu_baseline(prims: np.ndarray, key_bits: int, radius: int, sample: int, seconds: float = 10.0) -> dict:
-    """The CPU oracle (multithreaded restatement) on a bounded prefix sample,
-    built repeatedly for at least `seconds` of CPU work."""
+    """The CPU oracle (multithreaded restatement) on the whole workload (or
+    its first `sample` triangles when sample > 0), built repeatedly for at
+    least `seconds` of CPU work."""
     import oracle
     oracle.set_level_collapse(True)  # every stage on all host threads
-    m = min(sample, prims.shape[0])
+    m = min(sample, prims.shape[0]) if sample > 0 else prims.shape[0]
     sub = np.ascontiguousarray(prims[:m])
     builds, stage = 0, np.zeros(5)
     t = time.perf_counter()
@@ -167,8 +168,9 @@ def cpu_baseline(prims: np.ndarray, key_bits: int, radius: int, sample: int, sec
         stage += np.array(r["stage_ms"])
         builds += 1
     dt = time.perf_counter() - t
+    what = "all" if m == prims.shape[0] else "the first"
     return {"value": round(m * builds / dt / 1e6, 3), "unit": "Mtris/s", "cores": oracle.threads(), "kind": "port",
-            "sample": f"first {m:,} triangles of the workload, {builds} full CPU builds (bounds, Morton, radix sort, "
+            "sample": f"{what} {m:,} triangles of the workload, {builds} full CPU builds (bounds, Morton, radix sort, "
                       f"H-PLOC, BVH8) in {dt:.1f} s",
             "stage_ms": [round(x / builds, 1) for x in stage]}
 
@@ -376,9 +378,9 @@ def run_ours(args, world, rank, local):
                 "d2h_bytes_per_step": ctypes.sizeof(nxb.CResult),
                 "call": "nxb_build_bvh8 (C ABI, allocates outputs) after a pinned host->device copy"},
         # per build: bounds, Morton, the sort (30-bit: 4 passes; 63-bit: 4
-        # passes, the bucket sort and the fallback launch), H-PLOC, BVH8
-        # queue init, BVH8, finalize
-        "gpu_launches": (6 + (4 if key_bits == 30 else 6)) * args.steps,
+        # passes, the bucket sort and the fallback launch), H-PLOC (which
+        # also initialises the BVH8 work queue), BVH8, finalize
+        "gpu_launches": (5 + (4 if key_bits == 30 else 6)) * args.steps,
         "clocks": clk,
     }
     if not args.no_cpu_baseline:
@@ -581,7 +583,7 @@ def run_batch(args, world, rank, local):
     """Batched form: the batch1024 line."""
     b = measure_batch(args, world, rank, local, args.steps, args.warmup, autotune=not args.no_autotune,
                       fusion_sweep=not args.no_autotune, loop_baseline=not args.no_loop_baseline,
-                      cpu_baseline_tris=0 if args.no_cpu_baseline else args.cpu_sample)
+                      cpu_baseline_tris=0 if args.no_cpu_baseline else (args.cpu_sample or 1 << 62))
     if rank != 0:
         return
     pk = peaks()
@@ -822,7 +824,8 @@ def run_reference(args, world, rank, local):
     faulted (Xid 31) on the 4,194,304-triangle sphere with 30-bit keys.
     What is timed here is therefore the CPU restatement of the reference's
     algorithm (the oracle port) on all host cores, each step one CPU build
-    of a bounded prefix sample of the workload."""
+    of the whole workload (a prefix of it only when the steps would not
+    fit the time budget)."""
     if rank != 0:
         return
     if args.workload == "served":
@@ -840,26 +843,46 @@ def run_reference(args, world, rank, local):
         counts = scenes.batch_counts(meshes, seed=seed)
         prims_np = scenes.batch_meshes(counts, seed=seed)
         off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
-        # a prefix of whole meshes, each built on its own
-        last = int(np.searchsorted(off, min(args.cpu_sample, off[-1]), side="left"))
-        last = max(1, min(last, meshes))
-        subs = [np.ascontiguousarray(prims_np[off[i]:off[i + 1]]) for i in range(last) if counts[i]]
     else:
         prims_np = make_prims(args.workload)
-        subs = [np.ascontiguousarray(prims_np[:min(args.cpu_sample, prims_np.shape[0])])]
+        counts = np.array([prims_np.shape[0]])
+        off = np.array([0, prims_np.shape[0]], dtype=np.int64)
     n = prims_np.shape[0]
-    m = sum(x.shape[0] for x in subs)
-    sub = subs[0]
+
+    def sample_of(tris: int):
+        """The step's sample: the first `tris` triangles, each mesh built on
+        its own (a batch's meshes whole, one mesh cut at a prefix)."""
+        if len(counts) == 1:
+            return [np.ascontiguousarray(prims_np[:max(1, min(tris, n))])]
+        last = max(1, min(int(np.searchsorted(off, min(tris, off[-1]), side="left")), len(counts)))
+        return [np.ascontiguousarray(prims_np[off[i]:off[i + 1]]) for i in range(last) if counts[i]]
+
+    def step(subs):
+        st = np.zeros(5)
+        for x in subs:
+            r = oracle.build(x, key_bits, args.radius)
+            assert r["err"] == 0
+            st += np.array(r["stage_ms"])
+        return st
+
     for _ in range(args.warmup):
-        oracle.build(sub[: min(sub.shape[0], 65536)], key_bits, args.radius)
+        oracle.build(prims_np[: min(n, 65536)], key_bits, args.radius)
+    # Each step builds the whole workload when steps x (one whole build)
+    # fits the time budget, else the largest prefix that does: one whole
+    # build, untimed, measures it.
+    subs = sample_of(args.cpu_sample or n)
+    if not args.cpu_sample:
+        t = time.perf_counter()
+        step(subs)
+        t_full = time.perf_counter() - t
+        if args.steps * t_full > args.cpu_budget:
+            subs = sample_of(int(n * args.cpu_budget / (args.steps * t_full)))
+    m = sum(x.shape[0] for x in subs)
     times = []
     stage = np.zeros(5)
     for _ in range(args.steps):
         t = time.perf_counter()
-        for x in subs:
-            r = oracle.build(x, key_bits, args.radius)
-            assert r["err"] == 0
-            stage += np.array(r["stage_ms"])
+        stage += step(subs)
         times.append(time.perf_counter() - t)
     total = sum(times)
     value = m * args.steps / total / 1e6
@@ -871,8 +894,10 @@ def run_reference(args, world, rank, local):
             "config": {"workload": WORKLOADS[args.workload][0], "n_tris": n, "key_bits": key_bits,
                        "search_radius": args.radius, "sample_tris": m},
             "cpu_baseline": {"value": round(value, 3), "unit": "Mtris/s", "cores": oracle.threads(), "kind": "port",
-                             "sample": f"first {m:,} of the workload's {n:,} triangles per step, one full CPU build "
-                                       "(bounds, Morton, radix sort, H-PLOC, BVH8)",
+                             "sample": (f"all {n:,} triangles of the workload" if m == n else
+                                        f"first {m:,} of the workload's {n:,} triangles") +
+                                       " per step, one full CPU build (bounds, Morton, radix sort, H-PLOC, BVH8)"
+                                       + (" of each mesh" if len(counts) > 1 else ""),
                              "stage_ms": [round(x / args.steps, 1) for x in stage]},
             "e2e": {"value": round(value, 3), "unit": "Mtris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "reference path has no CPU implementation; its CUDA build faulted on GB300 (Xid 31, stale-L1 "
@@ -889,7 +914,11 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="clustered12m")
     ap.add_argument("--key-bits", type=int, choices=[30, 63], default=None)
     ap.add_argument("--radius", type=int, choices=[4, 8, 16], default=8)
-    ap.add_argument("--cpu-sample", type=int, default=2_000_000)
+    ap.add_argument("--cpu-sample", type=int, default=0,
+                    help="CPU builds: triangles per sample (0: the whole workload; the reference arm then shrinks it "
+                         "to a prefix only if --steps whole builds would exceed --cpu-budget)")
+    ap.add_argument("--cpu-budget", type=float, default=150.0,
+                    help="reference arm: seconds of timed CPU steps to aim below")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-loop-baseline", action="store_true",
                     help="batched workloads: leave out the loop-of-plain-builds comparison")
