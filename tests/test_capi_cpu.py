@@ -62,9 +62,10 @@ def test_workspace_sizes(lib):
         assert lib.nxb_query_build_sizes(n, ctypes.byref(cfg), ctypes.byref(s)) == 0
         assert s.bvh2_node_count == 2 * n - 1
         assert s.bvh8_node_capacity == (4 * n - 1 + 6) // 7
-        # keys x2, values x2, parent slots, BVH8 work slots, look-back
-        assert s.workspace_bytes >= n * (2 * kb + 8 + 4 + 8)
-        assert s.workspace_bytes < n * (2 * kb + 8 + 4 + 8 + 8)
+        # keys x2, values x2, parent slots, BVH8 work slots, H-PLOC cluster
+        # records, look-back
+        assert s.workspace_bytes >= n * (2 * kb + 8 + 4 + 8 + 32)
+        assert s.workspace_bytes < n * (2 * kb + 8 + 4 + 8 + 32 + 8)
     assert lib.nxb_query_build_sizes(0, None, ctypes.byref(s)) == 1
     # NXB_BUILD_VALIDATE belongs to the plain calls only
     v = nxb.BuildConfig(validate=True).to_c()
@@ -77,12 +78,13 @@ def test_validator_argument_checks_need_no_device(lib):
         return (b + 255) // 256 * 256
     n = 1000
     need2 = lib.nxb_validate_bvh2_scratch_bytes(n)
-    assert need2 == seg(8 * (2 * n - 1)) + seg(4 * (2 * n - 1)) + seg(4 * n)
+    # links, parent counts, leaf counts, one word per pointer-jumping round
+    assert need2 == seg(8 * (2 * n - 1)) + seg(4 * (2 * n - 1)) + seg(4 * n) + seg(4 * 32)
     assert lib.nxb_validate_bvh2_scratch_bytes(0) == 0
     assert lib.nxb_validate_bvh2_scratch_bytes(1 << 31) == 0
     m = 300
     need8 = lib.nxb_validate_bvh8_scratch_bytes(m, n)
-    assert need8 == seg(8 * m) + 3 * seg(4 * m) + seg(24 * m) + seg(4 * n)
+    assert need8 == seg(8 * m) + 3 * seg(4 * m) + seg(24 * m) + seg(4 * n) + seg(4 * 32)
     assert lib.nxb_validate_bvh8_scratch_bytes(0, n) == 0 and lib.nxb_validate_bvh8_scratch_bytes(m, 0) == 0
     # every call below is rejected before anything is enqueued
     assert lib.nxb_validate_bvh2(None, n, 0, 16, 16, need2, None) == 1
