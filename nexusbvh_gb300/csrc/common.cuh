@@ -69,6 +69,26 @@ __device__ __forceinline__ float half_area(const Box& b) {
     return __fmaf_rn(dz, dx, __fmaf_rn(dx, dy, dy * dz));
 }
 
+// half_area of two boxes at once, with Blackwell's paired f32x2 arithmetic:
+// the same operations in the same order, each rounded to nearest with
+// subnormals flushed (the library is built with --use_fast_math), so both
+// results have half_area's bits (checked by the numerics self-test).
+__device__ __forceinline__ void half_area2(const Box& a, const Box& b, float& ra, float& rb) {
+    auto pack = [](float lo, float hi) {
+        uint64_t r;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+        return r;
+    };
+    uint64_t dx, dy, dz, t;
+    asm("sub.rn.ftz.f32x2 %0, %1, %2;" : "=l"(dx) : "l"(pack(a.mx.x, b.mx.x)), "l"(pack(a.mn.x, b.mn.x)));
+    asm("sub.rn.ftz.f32x2 %0, %1, %2;" : "=l"(dy) : "l"(pack(a.mx.y, b.mx.y)), "l"(pack(a.mn.y, b.mn.y)));
+    asm("sub.rn.ftz.f32x2 %0, %1, %2;" : "=l"(dz) : "l"(pack(a.mx.z, b.mx.z)), "l"(pack(a.mn.z, b.mn.z)));
+    asm("mul.rn.ftz.f32x2 %0, %1, %2;" : "=l"(t) : "l"(dy), "l"(dz));
+    asm("fma.rn.ftz.f32x2 %0, %1, %2, %3;" : "=l"(t) : "l"(dx), "l"(dy), "l"(t));
+    asm("fma.rn.ftz.f32x2 %0, %1, %2, %3;" : "=l"(t) : "l"(dz), "l"(dx), "l"(t));
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(ra), "=f"(rb) : "l"(t));
+}
+
 // Float <-> monotone uint32 (for atomicMin/Max on floats without CAS
 // loops); -0 orders below +0.
 __device__ __forceinline__ uint32_t f2ord(float f) {

@@ -111,13 +111,24 @@ __global__ void fill_u32_kernel(uint32_t* p, uint32_t value, size_t count) {
 
 // ---- numerics self-test probes: the reference's plain source expressions
 // compiled with the same flags, next to the library's pinned forms.
-__global__ void probe_area_kernel(const float* boxes, uint32_t count, uint32_t* out) {
+__global__ void probe_area_kernel(const float* boxes, uint32_t count, uint32_t* out, uint32_t* paired_diff) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
     const float* f = boxes + 6 * i;
     Box b;
     b.mn = make_float3(f[0], f[1], f[2]);
     b.mx = make_float3(f[3], f[4], f[5]);
+    {
+        // the paired form against the single one, with box i^1 as partner
+        const float* g = boxes + 6 * (i ^ 1u);
+        Box c;
+        c.mn = make_float3(g[0], g[1], g[2]);
+        c.mx = make_float3(g[3], g[4], g[5]);
+        float rb, rc;
+        half_area2(b, c, rb, rc);
+        if (__float_as_uint(rb) != __float_as_uint(half_area(b)) || __float_as_uint(rc) != __float_as_uint(half_area(c)))
+            atomicAdd(paired_diff, 1u);
+    }
     const float dx = b.mx.x - b.mn.x, dy = b.mx.y - b.mn.y, dz = b.mx.z - b.mn.z;
     const float plain = dx * dy + dy * dz + dz * dx;  // AABB::Area, NXB AABB.h:46-50
     const float f0 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dy), __fmul_rn(dy, dz)), __fmul_rn(dz, dx));
@@ -193,7 +204,8 @@ cudaError_t launch_fill_u32(uint32_t* p, uint32_t value, size_t count, cudaStrea
 //  {254.5, 255, 255.25, 256, 256.5, 300, 511.75, -1.5};
 //  [20..23] bits of fminf(+0,-0), fminf(-0,+0), fmaxf(+0,-0), fmaxf(-0,+0);
 //  [24] divisions probed, [25] fast-math quotients != IEEE quotients,
-//  [26] of those, differences larger than 1 ulp.
+//  [26] of those, differences larger than 1 ulp;
+//  [27] boxes whose paired area (half_area2) differs from half_area.
 cudaError_t run_selftest(uint32_t* report) {
     const uint32_t nb = 1u << 16;
     std::vector<float> boxes(6 * nb);
@@ -204,9 +216,12 @@ cudaError_t run_selftest(uint32_t* report) {
     };
     for (uint32_t i = 0; i < nb; ++i) {
         float c[3], h[3];
+        // the last 4,096 boxes near the smallest normal floats, where
+        // flushing subnormal differences and products matters
+        const bool tiny = i >= nb - 4096;
         for (int a = 0; a < 3; ++a) {
-            c[a] = (rnd() - 0.5f) * 20.0f;
-            h[a] = rnd() * rnd() * 2.0f;
+            c[a] = (rnd() - 0.5f) * (tiny ? 4e-38f : 20.0f);
+            h[a] = rnd() * rnd() * (tiny ? 2e-38f : 2.0f);
         }
         for (int a = 0; a < 3; ++a) {
             boxes[6 * i + a] = c[a] - h[a];
@@ -229,21 +244,26 @@ cudaError_t run_selftest(uint32_t* report) {
         misc[3 * k + 2] = 0.25f + rnd() * 4.0f;
     }
     float *d_boxes = nullptr, *d_misc = nullptr;
-    uint32_t *d_out = nullptr, *d_out2 = nullptr;
+    uint32_t *d_out = nullptr, *d_out2 = nullptr, *d_paired = nullptr;
     cudaError_t e = cudaMalloc(&d_boxes, boxes.size() * 4);
+    if (!e) e = cudaMalloc(&d_paired, 4);
+    if (!e) e = cudaMemset(d_paired, 0, 4);
     if (!e) e = cudaMalloc(&d_misc, misc.size() * 4);
     if (!e) e = cudaMalloc(&d_out, (size_t)nb * 16);
     if (!e) e = cudaMalloc(&d_out2, (size_t)nm * 24);
     if (!e) e = cudaMemcpy(d_boxes, boxes.data(), boxes.size() * 4, cudaMemcpyHostToDevice);
     if (!e) e = cudaMemcpy(d_misc, misc.data(), misc.size() * 4, cudaMemcpyHostToDevice);
     if (!e) {
-        probe_area_kernel<<<(nb + 255) / 256, 256>>>(d_boxes, nb, d_out);
+        probe_area_kernel<<<(nb + 255) / 256, 256>>>(d_boxes, nb, d_out, d_paired);
         probe_misc_kernel<<<(nm + 255) / 256, 256>>>(d_misc, nm, d_out2);
         e = cudaGetLastError();
     }
     std::vector<uint32_t> o1((size_t)nb * 4), o2((size_t)nm * 6);
     if (!e) e = cudaMemcpy(o1.data(), d_out, o1.size() * 4, cudaMemcpyDeviceToHost);
     if (!e) e = cudaMemcpy(o2.data(), d_out2, o2.size() * 4, cudaMemcpyDeviceToHost);
+    uint32_t paired = 0;
+    if (!e) e = cudaMemcpy(&paired, d_paired, 4, cudaMemcpyDeviceToHost);
+    cudaFree(d_paired);
     cudaFree(d_boxes);
     cudaFree(d_misc);
     cudaFree(d_out);
@@ -269,6 +289,7 @@ cudaError_t run_selftest(uint32_t* report) {
             if ((q > r ? q - r : r - q) > 1) report[26]++;
         }
     }
+    report[27] = paired;
     return cudaSuccess;
 }
 

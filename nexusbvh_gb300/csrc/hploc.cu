@@ -135,6 +135,17 @@ __device__ __forceinline__ uint32_t nearest_neighbour(uint32_t num, const Box& c
             grow(u, lo_box);
             return __float_as_uint(half_area(u));
         };
+        // two pairs' areas at once (half_area2)
+        auto pair2 = [&](const Box& lo0, const Box& hi0, uint32_t a0, uint32_t d0, const Box& lo1, const Box& hi1,
+                         uint32_t a1, uint32_t d1, uint32_t& f0, uint32_t& f1) {
+            Box u0 = hi0, u1 = hi1;
+            grow(u0, lo0);
+            grow(u1, lo1);
+            float r0, r1;
+            half_area2(u0, u1, r0, r1);
+            f0 = ((lane + a0) & 31u) + d0 >= num ? kInvalid : __float_as_uint(r0);
+            f1 = ((lane + a1) & 31u) + d1 >= num ? kInvalid : __float_as_uint(r1);
+        };
         auto pick = [&](uint32_t f, uint32_t a, uint32_t d) {
             const uint32_t fwd = a ? __shfl_sync(kFullMask, f, (lane - a) & 31u) : f;
             const uint32_t back = __shfl_sync(kFullMask, f, (lane - d - a) & 31u);
@@ -149,14 +160,19 @@ __device__ __forceinline__ uint32_t nearest_neighbour(uint32_t num, const Box& c
         };
         const Box b1 = fetch(1);
         const Box b2 = fetch(2);
-        pick(pair(cb, b1, 0, 1), 0, 1);
-        pick(pair(cb, b2, 0, 2), 0, 2);
+        {
+            uint32_t f1, f2;
+            pair2(cb, b1, 0, 1, cb, b2, 0, 2, f1, f2);
+            pick(f1, 0, 1);
+            pick(f2, 0, 2);
+        }
         {
             const Box b5 = fetch(5);
-            const uint32_t f3 = pair(b2, b5, 2, 3), f4 = pair(b1, b5, 1, 4), f5 = pair(cb, b5, 0, 5);
+            uint32_t f3, f4;
+            pair2(b2, b5, 2, 3, b1, b5, 1, 4, f3, f4);
             pick(f3, 2, 3);
             pick(f4, 1, 4);
-            pick(f5, 0, 5);
+            pick(pair(cb, b5, 0, 5), 0, 5);
         }
         {
             const Box b8 = fetch(8);
@@ -170,24 +186,26 @@ __device__ __forceinline__ uint32_t nearest_neighbour(uint32_t num, const Box& c
             // against the boxes of lanes +9, +10, +13 and +16
             {
                 const Box b9 = fetch(9);
-                pick(pair(cb, b9, 0, 9), 0, 9);
-            }
-            {
                 const Box b10 = fetch(10);
-                pick(pair(cb, b10, 0, 10), 0, 10);
+                uint32_t f9, f10;
+                pair2(cb, b9, 0, 9, cb, b10, 0, 10, f9, f10);
+                pick(f9, 0, 9);
+                pick(f10, 0, 10);
             }
             {
                 const Box b13 = fetch(13);
-                const uint32_t f11 = pair(b2, b13, 2, 11), f12 = pair(b1, b13, 1, 12), f13 = pair(cb, b13, 0, 13);
+                uint32_t f11, f12;
+                pair2(b2, b13, 2, 11, b1, b13, 1, 12, f11, f12);
                 pick(f11, 2, 11);
                 pick(f12, 1, 12);
-                pick(f13, 0, 13);
+                pick(pair(cb, b13, 0, 13), 0, 13);
             }
             const Box b16 = fetch(16);
-            const uint32_t f14 = pair(b2, b16, 2, 14), f15 = pair(b1, b16, 1, 15), f16 = pair(cb, b16, 0, 16);
+            uint32_t f14, f15;
+            pair2(b2, b16, 2, 14, b1, b16, 1, 15, f14, f15);
             pick(f14, 2, 14);
             pick(f15, 1, 15);
-            pick(f16, 0, 16);
+            pick(pair(cb, b16, 0, 16), 0, 16);
         }
     } else {
 #pragma unroll

@@ -207,6 +207,7 @@ def test_numerics_selftest(gpu, orc):
     rep = nxb.selftest_numerics()
     assert rep[0] > 0
     assert rep[3] == 0, "pinned area form differs from the plain expression under --use_fast_math"
+    assert rep[27] == 0, "paired f32x2 area differs from the single-box area"
     values = [254.5, 255.0, 255.25, 256.0, 256.5, 300.0, 511.75, -1.5]
     import math
     for k, v in enumerate(values):
