@@ -176,10 +176,11 @@ __device__ __forceinline__ uint32_t nearest_neighbour(uint32_t num, const Box& c
         }
         {
             const Box b8 = fetch(8);
-            const uint32_t f6 = pair(b2, b8, 2, 6), f7 = pair(b1, b8, 1, 7), f8 = pair(cb, b8, 0, 8);
+            uint32_t f6, f7;
+            pair2(b2, b8, 2, 6, b1, b8, 1, 7, f6, f7);
             pick(f6, 2, 6);
             pick(f7, 1, 7);
-            pick(f8, 0, 8);
+            pick(pair(cb, b8, 0, 8), 0, 8);
         }
         if constexpr (R == 16) {
             // distances 9..16 are 8 + (1..8): the same low boxes 0, 1, 2

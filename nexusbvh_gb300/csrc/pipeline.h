@@ -16,10 +16,14 @@ namespace nxb {
 // keys (30-bit codes and a 10-bit mesh index).
 constexpr int kMaxSortPasses = 10;
 
-// BVH8 work-queue counters, each on its own 128-byte line (they are polled
-// and bumped by every warp): next slot to claim, BVH8 nodes, leaves, work
-// slots allocated, work items allocated but not finished.
-constexpr int kBvh8Claim = 0, kBvh8Nodes = 32, kBvh8Leaves = 64, kBvh8Alloc = 96, kBvh8Pending = 128;
+// BVH8 work-queue counters (they are polled and bumped by every warp):
+// next slot to claim; one 64-bit word of work slots allocated (low half)
+// and leaves (high half), bumped with one atomic, where one mesh's BVH8
+// nodes are its slots (every internal node is one work item, root
+// included); work items allocated but not finished.  Each counter has its
+// own 128-byte line.
+constexpr int kBvh8Claim = 0, kBvh8Alloc = 32, kBvh8Nodes = kBvh8Alloc, kBvh8Leaves = kBvh8Alloc + 1,
+              kBvh8Pending = 64;
 constexpr int kBvh8CtrWords = 160;
 
 // The BVH8 work queue of an n-primitive build before the collapse: slot 0
@@ -30,9 +34,8 @@ __device__ __forceinline__ uint64_t bvh8_queue_slot(uint32_t i, uint32_t n) {
 }
 __device__ __forceinline__ void bvh8_queue_counters(uint32_t* ctr) {
     ctr[kBvh8Claim] = 0;
-    ctr[kBvh8Nodes] = 1;
+    ctr[kBvh8Alloc] = 1;  // = kBvh8Nodes: the root
     ctr[kBvh8Leaves] = 0;
-    ctr[kBvh8Alloc] = 1;
     ctr[kBvh8Pending] = 1;
 }
 constexpr int kRadixBits = 8;

@@ -284,9 +284,8 @@ __global__ void bvh8_batch_init_kernel(uint64_t* pairs, uint32_t slots, MeshBatc
         uint32_t* c = ctr + i0 * kBvh8CtrWords;
         const uint32_t meshes = groups.mesh[i0 + 1] - groups.mesh[i0];
         c[kBvh8Claim] = 0;
-        c[kBvh8Nodes] = 0;
+        c[kBvh8Alloc] = meshes;  // a batch counts nodes and leaves per mesh
         c[kBvh8Leaves] = 0;
-        c[kBvh8Alloc] = meshes;
         c[kBvh8Pending] = meshes;
     }
 }
@@ -477,16 +476,16 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
             if (lane >= (uint32_t)o) incl += y;
         }
         const uint32_t done = __popc(__ballot_sync(kFullMask, ready));
-        uint32_t bases[3] = {0, 0, 0};
+        // one 64-bit atomic: work slots (one mesh: = BVH8 nodes) low, leaves high
+        uint64_t bases = 0;
         if (lane == 31) {
-            const uint32_t tn = incl & 0x3FFu, tl = (incl >> 10) & 0x3FFu, tw = incl >> 20;
-            if (tn) bases[0] = atomicAdd(ctr + kBvh8Nodes, tn);
-            if (tl) bases[1] = atomicAdd(ctr + kBvh8Leaves, tl);
-            if (tw) bases[2] = atomicAdd(ctr + kBvh8Alloc, tw);
+            const uint64_t tl = (incl >> 10) & 0x3FFu, tw = incl >> 20;
+            if (tl | tw)
+                bases = atomicAdd(reinterpret_cast<unsigned long long*>(ctr + kBvh8Alloc),
+                                  (unsigned long long)((tl << 32) | tw));
         }
-        const uint32_t nb = __shfl_sync(kFullMask, bases[0], 31);
-        const uint32_t lb = __shfl_sync(kFullMask, bases[1], 31);
-        const uint32_t wb = __shfl_sync(kFullMask, bases[2], 31);
+        bases = __shfl_sync(kFullMask, bases, 31);
+        const uint32_t wb = (uint32_t)bases, nb = wb, lb = (uint32_t)(bases >> 32);
         if (internal) {
             const uint32_t excl = incl - packed;
             uint32_t child_base, prim_base;
@@ -572,7 +571,6 @@ cudaError_t run_bvh8_stall_probe(uint32_t* err_out) {
     e = cudaMemset(buf, 0, bytes);
     if (!e) e = cudaMemset(pairs, 0xFF, 8 * n);
     uint32_t c[kBvh8CtrWords] = {};
-    c[kBvh8Nodes] = 1;
     c[kBvh8Alloc] = 1;    // slot 0 is allocated ...
     c[kBvh8Pending] = 1;  // ... but its pair is never written
     if (!e) e = cudaMemcpy(ctr, c, sizeof(c), cudaMemcpyHostToDevice);
