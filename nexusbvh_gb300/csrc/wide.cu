@@ -296,9 +296,15 @@ __global__ void bvh8_batch_init_kernel(uint64_t* pairs, uint32_t slots, MeshBatc
 // reference does (one per primitive, each re-reading the leaf node).  Every
 // inner child gets a fresh slot (breadth-first), so a slot is always written
 // by an item in a lower slot.  Each lane holds one slot at a time and claims
-// the next one (warp-aggregated) once its item is done, but only among the
-// slots already allocated, which are ready or about to be; the kernel ends
-// when the count of allocated-but-unfinished items drops to zero.
+// the next one (warp-aggregated: one atomic on the claim counter) once its
+// item is done, whether or not a parent has allocated it yet, and polls it
+// until its item arrives; a slot is only ever waited on by its own lane, so
+// lanes that wait hold no other lane up.  The kernel ends when the count of
+// allocated-but-unfinished items drops to zero (the slots still held then
+// are never allocated).  Claiming without first reading the allocation
+// counter keeps two loads per warp pass off the counters' cache lines,
+// which every warp of the grid hits (measured on GB300: BVH8 0.858 ->
+// 0.836 ms at 12.58M clustered triangles, 0.340 -> 0.320 ms at 4.19M).
 // An item is (mesh-local BVH2 index << 32 | BVH8 index in `out`).  In the
 // batched form (Seg = MeshBatch) the items of all meshes share the queue,
 // the BVH8 index names the mesh, and nodes and leaves are counted per mesh
@@ -326,31 +332,21 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
     bool retired = false;
     uint32_t idle = 0;
     for (;;) {
-        // lanes without a slot claim the next ones, in increasing order, but
-        // only slots a parent has already allocated (so they are ready, or
-        // about to be): a lane never sits on a slot of a subtree that does
-        // not exist yet while its warp's other lanes have work
+        // lanes without a slot claim the next ones, in increasing order; a
+        // slot past the queue's end is never allocated and retires the lane
         const bool want = !retired && slot == kInvalid;
         const uint32_t wmask = __ballot_sync(kFullMask, want);
         if (wmask) {
             const uint32_t leader = __ffs(wmask) - 1;
-            uint32_t base = 0, got = 0;
-            if (lane == leader) {
-                const uint32_t claimed = ld_relaxed_u32(ctr + kBvh8Claim);
-                const uint32_t alloc = ld_relaxed_u32(ctr + kBvh8Alloc);
-                const uint32_t avail = alloc > claimed ? alloc - claimed : 0u;
-                got = min((uint32_t)__popc(wmask), avail);
-                if (got) base = atomicAdd(ctr + kBvh8Claim, got);
-            }
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(ctr + kBvh8Claim, (uint32_t)__popc(wmask));
             base = __shfl_sync(kFullMask, base, leader);
-            got = __shfl_sync(kFullMask, got, leader);
-            const uint32_t rank = __popc(wmask & lanemask_lt());
-            if (want && rank < got) {
-                slot = base + rank;
-                if (slot >= slots) {
-                    slot = kInvalid;
+            if (want) {
+                const uint32_t claimed = base + __popc(wmask & lanemask_lt());
+                if (claimed < slots && claimed >= base)
+                    slot = claimed;
+                else
                     retired = true;
-                }
             }
         }
         if (__all_sync(kFullMask, retired)) return;
