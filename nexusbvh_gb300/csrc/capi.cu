@@ -56,7 +56,7 @@ struct Layout {
     SortPlan plan{};
     size_t tiles_words = 0;  // look-back words for all passes
     size_t ctrl = 0, result = 0, cost = 0, keys_a = 0, keys_b = 0, vals_a = 0, vals_b = 0, lookback = 0, parent = 0,
-           pairs = 0, records = 0, total = 0;
+           pairs = 0, records = 0, kids = 0, total = 0;
 };
 
 Layout make_layout(uint32_t n, uint32_t key_bits) {
@@ -87,6 +87,7 @@ Layout make_layout(uint32_t n, uint32_t key_bits) {
     L.parent = seg(4ull * n);
     L.pairs = seg(8ull * n);
     L.records = seg(32ull * n);
+    L.kids = seg(64ull * n);
     L.total = off;
     return L;
 }
@@ -195,15 +196,18 @@ nxb_status enqueue_build(const void* prims, nxb_prim_type type, uint32_t n, cons
     // an even number of passes leaves the sorted keys / permutation in A
     NXB_TRY(mark(3));
     // the sort's second value buffer holds the H-PLOC cluster tokens
+    // with a BVH8 to build, the climb also writes each internal node's
+    // children side by side, which the collapse reads instead of the BVH2
+    ChildPair* kids = bvh8 ? reinterpret_cast<ChildPair*>(ws + L.kids) : nullptr;
     NXB_TRY(launch_hploc(L.key_bytes, keys_a, vals_a, parent, bvh2, n, radius_of(cfg), vals_b,
                          &ctrl->parent_of_last, &ctrl->hploc_leaf_ctr, &ctrl->error_word, s,
                          reinterpret_cast<Node2*>(ws + L.records), bvh8 ? pairs : nullptr,
-                         bvh8 ? ctrl->bvh8_ctr : nullptr));
+                         bvh8 ? ctrl->bvh8_ctr : nullptr, kids));
     NXB_TRY(mark(4));
     if (bvh8) {
         // the climb initialised the collapse's work queue
         NXB_TRY(launch_bvh8(bvh2, n, bvh8, (uint32_t)bvh8_capacity(n), prim_idx, pairs, ctrl->bvh8_ctr,
-                            &ctrl->error_word, auction_of(cfg), s));
+                            &ctrl->error_word, auction_of(cfg), s, kids));
     }
     NXB_TRY(mark(5));
     if (result) NXB_TRY(launch_finalize(ctrl, result, n, s));

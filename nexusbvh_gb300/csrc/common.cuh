@@ -173,6 +173,43 @@ __device__ __forceinline__ void store_node(Node2* nodes, uint32_t i, const Box& 
     p[1] = make_float4(b.mx.y, b.mx.z, __uint_as_float(l), __uint_as_float(r));
 }
 
+// The two children of an internal BVH2 node X side by side: both boxes and
+// both indices in one 64-byte record (at X - n), written by the merge that
+// creates X.  The BVH8 collapse opens X with this one aligned load instead
+// of reading X's node and then both child nodes; X's own box is the union
+// of the two, exactly (every internal box is computed as that union).
+struct __align__(64) ChildPair {
+    Box l, r;
+    uint32_t li, ri;
+    uint32_t pad[2];
+};
+static_assert(sizeof(ChildPair) == 64, "child pair record");
+
+__device__ __forceinline__ void store_child_pair(ChildPair* p, const Box& l, const Box& r, uint32_t li,
+                                                 uint32_t ri) {
+    uint4* q = reinterpret_cast<uint4*>(p);
+    __stcg(q, make_uint4(__float_as_uint(l.mn.x), __float_as_uint(l.mn.y), __float_as_uint(l.mn.z),
+                         __float_as_uint(l.mx.x)));
+    __stcg(q + 1, make_uint4(__float_as_uint(l.mx.y), __float_as_uint(l.mx.z), __float_as_uint(r.mn.x),
+                             __float_as_uint(r.mn.y)));
+    __stcg(q + 2, make_uint4(__float_as_uint(r.mn.z), __float_as_uint(r.mx.x), __float_as_uint(r.mx.y),
+                             __float_as_uint(r.mx.z)));
+    __stcg(q + 3, make_uint4(li, ri, 0u, 0u));
+}
+// Through the read-only path: the records are finished by an earlier kernel.
+__device__ __forceinline__ ChildPair load_child_pair(const ChildPair* p) {
+    const uint4* q = reinterpret_cast<const uint4*>(p);
+    const uint4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2), d = __ldg(q + 3);
+    ChildPair r;
+    r.l.mn = make_float3(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z));
+    r.l.mx = make_float3(__uint_as_float(a.w), __uint_as_float(b.x), __uint_as_float(b.y));
+    r.r.mn = make_float3(__uint_as_float(b.z), __uint_as_float(b.w), __uint_as_float(c.x));
+    r.r.mx = make_float3(__uint_as_float(c.y), __uint_as_float(c.z), __uint_as_float(c.w));
+    r.li = d.x;
+    r.ri = d.y;
+    return r;
+}
+
 __device__ __forceinline__ Box shfl_box(const Box& b, uint32_t src) {
     Box r;
     r.mn.x = __shfl_sync(kFullMask, b.mn.x, src);

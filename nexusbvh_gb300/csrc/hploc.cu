@@ -235,6 +235,7 @@ struct MergeCtx {
     Node2* nodes;
     uint32_t* tok;             // first-leaf token of each stored cluster
     Node2* rec;                // if not null: stored clusters as {box, id, token} records
+    ChildPair* kids;           // if not null: each internal node's two children, at node - n
     uint32_t* parent_of_last;  // node whose child is node 2n-2 (root fix-up)
     uint32_t n;
     uint32_t node_limit;       // 2n-1
@@ -277,9 +278,11 @@ __device__ __forceinline__ uint32_t merge_step(const MergeCtx& m, uint32_t num, 
         nb = shfl_box(cb, nn & 31u);
     }
     if (merge) {
-        grow(cb, nb);
         const uint32_t idx = m.n - 1 + ntok;
-        if (idx < m.node_limit && ntok != 0) {
+        const bool ok = idx < m.node_limit && ntok != 0;
+        if (ok && m.kids) store_child_pair(m.kids + (idx - m.n), cb, nb, cid, ncid);
+        grow(cb, nb);
+        if (ok) {
             store_node(m.nodes, idx, cb, cid, ncid);
             if (cid == m.node_limit - 1 || ncid == m.node_limit - 1) atomicExch(m.parent_of_last, idx);
         } else {
@@ -326,7 +329,6 @@ __device__ __forceinline__ void merge_root(const MergeCtx& m, uint32_t& cid, uin
         const uint32_t root = m.node_limit - 1;
         const uint32_t natural = m.n - 1 + b_tok;
         uint32_t a = cid, b = b_cid;
-        grow(cb, b_box);
         if (natural != root) {
             if (natural >= m.node_limit) {
                 set_error(m.err, NXB_DEVERR_HPLOC_INVALID_CLUSTER);
@@ -336,24 +338,34 @@ __device__ __forceinline__ void merge_root(const MergeCtx& m, uint32_t& cid, uin
                 const uint4 lo = __ldcg(src), hi = __ldcg(src + 1);
                 __stcg(dst, lo);
                 __stcg(dst + 1, hi);
+                if (m.kids) {  // the moved node's child pair moves with it
+                    const uint4* ks = reinterpret_cast<const uint4*>(m.kids + (root - m.n));
+                    uint4* kd = reinterpret_cast<uint4*>(m.kids + (natural - m.n));
+                    const uint4 k0 = __ldcg(ks), k1 = __ldcg(ks + 1), k2 = __ldcg(ks + 2), k3 = __ldcg(ks + 3);
+                    __stcg(kd, k0);
+                    __stcg(kd + 1, k1);
+                    __stcg(kd + 2, k2);
+                    __stcg(kd + 3, k3);
+                }
                 if (a == root) {
                     a = natural;
                 } else if (b == root) {
                     b = natural;
                 } else {
                     const uint32_t p = __ldcg(m.parent_of_last);
-                    if (p < m.node_limit) {
+                    if (p < m.node_limit && p >= m.n) {
                         uint32_t* pl = reinterpret_cast<uint32_t*>(m.nodes + p) + 6;
-                        if (__ldcg(pl) == root)
-                            __stcg(pl, natural);
-                        else
-                            __stcg(pl + 1, natural);
+                        const uint32_t side = __ldcg(pl) == root ? 0u : 1u;
+                        __stcg(pl + side, natural);
+                        if (m.kids) __stcg(&m.kids[p - m.n].li + side, natural);
                     } else {
                         set_error(m.err, NXB_DEVERR_HPLOC_INVALID_CLUSTER);
                     }
                 }
             }
         }
+        if (m.kids) store_child_pair(m.kids + (root - m.n), cb, b_box, a, b);
+        grow(cb, b_box);
         store_node(m.nodes, root, cb, a, b);
         cid = root;
     }
@@ -369,8 +381,8 @@ __device__ __forceinline__ MergeCtx mesh_ctx(const MergeCtx& all, const Seg& seg
         const uint32_t mesh = __shfl_sync(kFullMask, me.m, owner);
         start = __shfl_sync(kFullMask, me.start, owner);
         const uint32_t count = __shfl_sync(kFullMask, me.count, owner);
-        return MergeCtx{all.nodes + 2ull * start, all.tok, all.rec, all.parent_of_last + mesh, count, 2 * count - 1,
-                        all.err};
+        return MergeCtx{all.nodes + 2ull * start, all.tok, all.rec, nullptr, all.parent_of_last + mesh, count,
+                        2 * count - 1, all.err};
     } else {
         start = 0;
         return all;
@@ -544,10 +556,10 @@ __global__ __launch_bounds__(kThreads, hploc_ctas_per_sm<R, Seg>()) void hploc_k
                                                          uint32_t* parent, Node2* nodes, Seg seg, uint32_t begin,
                                                          uint32_t* tok, uint32_t* parent_of_last, uint32_t* leaf_ctr,
                                                          uint32_t* err, uint32_t end, uint32_t chunk, Node2* rec,
-                                                         uint64_t* bvh8_pairs, uint32_t* bvh8_ctr) {
+                                                         uint64_t* bvh8_pairs, uint32_t* bvh8_ctr, ChildPair* kids) {
     const uint32_t lane = lane_id();
     if (!Seg::kBatch && bvh8_ctr && blockIdx.x == 0 && threadIdx.x == 0) bvh8_queue_counters(bvh8_ctr);
-    const MergeCtx all{nodes, tok, rec, parent_of_last, end, 2 * end - 1, err};
+    const MergeCtx all{nodes, tok, rec, Seg::kBatch ? nullptr : kids, parent_of_last, end, 2 * end - 1, err};
     // each warp's row for the merge compaction (single-mesh builds)
     __shared__ uint4 s_rows[Seg::kBatch ? 1 : kThreads / 32][64];
     uint4* row = s_rows[Seg::kBatch ? 0 : threadIdx.x >> 5];
@@ -557,6 +569,7 @@ __global__ __launch_bounds__(kThreads, hploc_ctas_per_sm<R, Seg>()) void hploc_k
     bool active = false;
     uint32_t chunk_next = 0, chunk_end = 0;  // warp-uniform
     bool exhausted = false;                  // warp-uniform
+    bool release_due = false;                // warp-uniform: a pass merged, its release fence is pending
     for (;;) {
         // refill stopped lanes with fresh leaves
         uint32_t need = __ballot_sync(kFullMask, !active);
@@ -587,13 +600,25 @@ __global__ __launch_bounds__(kThreads, hploc_ctas_per_sm<R, Seg>()) void hploc_k
             chunk_next += took;
             need = __ballot_sync(kFullMask, !active);
         }
-        if (!__any_sync(kFullMask, active)) return;
+        if (!__any_sync(kFullMask, active)) {
+            if (release_due) fence_acq_rel_gpu();
+            return;
+        }
         bool second = false;
+        bool go_right = false;
+        if (active)
+            go_right = left == me.start ||
+                       (right != me.start + me.count - 1 &&
+                        delta(keys, right, right + 1, me.start) < delta(keys, left - 1, left, me.start));
+        if (release_due) {
+            // release: the previous pass's clusters and nodes before this
+            // pass's hand-overs (the store drain overlaps the refill and the
+            // key loads above)
+            fence_acq_rel_gpu();
+            release_due = false;
+        }
         if (active) {
             uint32_t prev;
-            const bool go_right = left == me.start ||
-                                  (right != me.start + me.count - 1 &&
-                                   delta(keys, right, right + 1, me.start) < delta(keys, left - 1, left, me.start));
             if (go_right) {
                 prev = atomicExch(parent + right, left);
                 if (prev != kInvalid) {
@@ -620,8 +645,8 @@ __global__ __launch_bounds__(kThreads, hploc_ctas_per_sm<R, Seg>()) void hploc_k
                 ploc_merge<R, Seg>(owner, left, right, split, final, me, cluster, all, seg, row);
                 todo &= todo - 1;
             }
-            __syncwarp();
-            fence_acq_rel_gpu();  // release: clusters and nodes before the next hand-over
+            __syncwarp();  // every lane's stores before the owners' next hand-overs
+            release_due = true;
         }
     }
 }
@@ -629,7 +654,8 @@ __global__ __launch_bounds__(kThreads, hploc_ctas_per_sm<R, Seg>()) void hploc_k
 template <typename K, int R, typename Seg>
 cudaError_t launch_r(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, Seg seg, uint32_t begin,
                      uint32_t end, uint32_t* tok, uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err,
-                     uint32_t max_per_sm, cudaStream_t s, Node2* rec, uint64_t* pairs, uint32_t* ctr) {
+                     uint32_t max_per_sm, cudaStream_t s, Node2* rec, uint64_t* pairs, uint32_t* ctr,
+                     ChildPair* kids) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hploc_kernel<K, R, Seg>, kThreads, 0);
     if (max_per_sm && (uint32_t)per_sm > max_per_sm) per_sm = (int)max_per_sm;
@@ -638,7 +664,7 @@ cudaError_t launch_r(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* 
     const uint32_t grid = std::max(1u, std::min(want, (uint32_t)(device_info().sms * per_sm)));
     const uint32_t chunk = leaf_chunk(end - begin, grid * (kThreads / 32), Seg::kBatch);
     hploc_kernel<K, R, Seg><<<grid, kThreads, 0, s>>>(keys, cluster, parent, nodes, seg, begin, tok, pol, leaf_ctr,
-                                                      err, end, chunk, rec, pairs, ctr);
+                                                      err, end, chunk, rec, pairs, ctr, kids);
     return cudaGetLastError();
 }
 
@@ -646,17 +672,17 @@ template <typename K, typename Seg>
 cudaError_t launch_t(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* nodes, Seg seg, uint32_t begin,
                      uint32_t end, uint32_t radius, uint32_t* tok, uint32_t* pol, uint32_t* leaf_ctr, uint32_t* err,
                      uint32_t max_per_sm, cudaStream_t s, Node2* rec = nullptr, uint64_t* pairs = nullptr,
-                     uint32_t* ctr = nullptr) {
+                     uint32_t* ctr = nullptr, ChildPair* kids = nullptr) {
     switch (radius) {
         case 4:
             return launch_r<K, 4>(keys, cluster, parent, nodes, seg, begin, end, tok, pol, leaf_ctr, err, max_per_sm,
-                                  s, rec, pairs, ctr);
+                                  s, rec, pairs, ctr, kids);
         case 16:
             return launch_r<K, 16>(keys, cluster, parent, nodes, seg, begin, end, tok, pol, leaf_ctr, err,
-                                   max_per_sm, s, rec, pairs, ctr);
+                                   max_per_sm, s, rec, pairs, ctr, kids);
         default:
             return launch_r<K, 8>(keys, cluster, parent, nodes, seg, begin, end, tok, pol, leaf_ctr, err, max_per_sm,
-                                  s, rec, pairs, ctr);
+                                  s, rec, pairs, ctr, kids);
     }
 }
 
@@ -664,14 +690,15 @@ cudaError_t launch_t(const K* keys, uint32_t* cluster, uint32_t* parent, Node2* 
 
 cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
                          uint32_t n, uint32_t radius, uint32_t* tokens, uint32_t* parent_of_last, uint32_t* leaf_ctr,
-                         uint32_t* err, cudaStream_t s, Node2* records, uint64_t* bvh8_pairs, uint32_t* bvh8_ctr) {
+                         uint32_t* err, cudaStream_t s, Node2* records, uint64_t* bvh8_pairs, uint32_t* bvh8_ctr,
+                         ChildPair* child_pairs) {
     const SingleMesh seg{n};
     if (!bvh8_pairs != !bvh8_ctr) return cudaErrorInvalidValue;
     if (key_bytes == 4)
         return launch_t((const uint32_t*)keys, cluster_idx, parent, nodes, seg, 0u, n, radius, tokens,
-                        parent_of_last, leaf_ctr, err, 0u, s, records, bvh8_pairs, bvh8_ctr);
+                        parent_of_last, leaf_ctr, err, 0u, s, records, bvh8_pairs, bvh8_ctr, child_pairs);
     return launch_t((const uint64_t*)keys, cluster_idx, parent, nodes, seg, 0u, n, radius, tokens, parent_of_last,
-                    leaf_ctr, err, 0u, s, records, bvh8_pairs, bvh8_ctr);
+                    leaf_ctr, err, 0u, s, records, bvh8_pairs, bvh8_ctr, child_pairs);
 }
 
 cudaError_t launch_hploc_batch(const uint64_t* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,

@@ -181,17 +181,23 @@ cudaError_t launch_sort63_hybrid(const uint64_t* keys_in, const uint32_t* vals_i
 // which the climb initialises as launch_bvh8_init would (each lane writes
 // the slot of the leaf it takes), so that the collapse can follow without
 // an initialisation launch of its own.
+// child_pairs (optional): n-1 records of 64 bytes, 64-byte aligned; record
+// X - n receives the children of internal node X (boxes and indices), for
+// launch_bvh8 to read instead of the BVH2 nodes.
 cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
                          uint32_t n, uint32_t radius, uint32_t* tokens, uint32_t* parent_of_last, uint32_t* leaf_ctr,
                          uint32_t* err, cudaStream_t s, Node2* records, uint64_t* bvh8_pairs = nullptr,
-                         uint32_t* bvh8_ctr = nullptr);
+                         uint32_t* bvh8_ctr = nullptr, ChildPair* child_pairs = nullptr);
 // ---------------------------------------------------------------- stage 5
 // pairs: n uint64 slots; ctr: kBvh8CtrWords words (128-byte aligned).
 // Both are initialised by launch_bvh8_init.
 cudaError_t launch_bvh8_init(uint64_t* pairs, uint32_t n, uint32_t* ctr, cudaStream_t s);
 // auction: the reference's USE_AUCTION slot assignment instead of the greedy one.
+// child_pairs (optional): the records launch_hploc wrote for this BVH2; the
+// collapse then opens nodes through them and reads no BVH2 node.
 cudaError_t launch_bvh8(const Node2* bvh2, uint32_t n, Node8* out, uint32_t cap, uint32_t* prim_idx, uint64_t* pairs,
-                        uint32_t* ctr, uint32_t* err, bool auction, cudaStream_t s);
+                        uint32_t* ctr, uint32_t* err, bool auction, cudaStream_t s,
+                        const ChildPair* child_pairs = nullptr);
 // ---------------------------------------------------------------- batches
 // The same stages over independent meshes laid end to end (MeshBatch in
 // common.cuh): one launch per stage for the whole batch.

@@ -15,7 +15,15 @@
 //   * each thread keeps the children it expands in a slot table in shared
 //     memory (BVH2 index, children, box), so popping a child, the slot
 //     assignment and the quantisation never reload a node (the reference
-//     reloads each child box up to three times).
+//     reloads each child box up to three times);
+//   * in a whole-pipeline build the H-PLOC merges also write each internal
+//     node's two children side by side (ChildPair, 64 bytes): the collapse
+//     then opens a node with one aligned load of its record and reads no
+//     BVH2 node at all (a leaf child's box is in its parent's record).
+//     Measured on GB300 at 12.58M clustered triangles: BVH8 0.833 ->
+//     0.553 ms, H-PLOC 2.16 -> 2.34 ms (the records' stores), build 3.91 ->
+//     3.81 ms; the BVH8 kernel's time hardly depends on its occupancy (3 / 6
+//     CTAs per SM: 0.898 / 0.833 ms), it follows the random node traffic.
 // The decisions are the reference's:
 //   * expansion always re-opens the highest-indexed inner child, the child
 //     with the smaller area going to the re-opened position (:284-330);
@@ -37,8 +45,9 @@ constexpr uint32_t kQueueSpinLimit = 1u << 20;
 constexpr uint32_t kFallback = 0xFFFFFFFEu;  // auction_assign: use the greedy assignment
 // Opening a BVH2 node needs its children; the opens of one item form a chain
 // of dependent loads.  With prefetching on, loading a child that is itself
-// internal also asks L2 for that child's two children, so that the next open
-// (or the child's own work item) finds them there.
+// internal also asks L2 for that child's two children (or, with child-pair
+// records, for the child's record), so that the next open (or the child's
+// own work item) finds them there.
 constexpr bool kPrefetch = true;
 constexpr int kSlotWords = 9;  // BVH2 index, left, right, box (6 floats)
 constexpr size_t kSlotSmem = (size_t)kThreads * 8 * kSlotWords * sizeof(uint32_t);
@@ -83,6 +92,17 @@ struct SlotTable {
         *at(slot, 6) = __float_as_uint(nd.b.mx.x);
         *at(slot, 7) = __float_as_uint(nd.b.mx.y);
         *at(slot, 8) = __float_as_uint(nd.b.mx.z);
+    }
+    // child-pair builds: the index and the box (the children come from the
+    // node's own record when it is opened)
+    __device__ void put(uint32_t slot, uint32_t idx, const Box& b) const {
+        *at(slot, 0) = idx;
+        *at(slot, 3) = __float_as_uint(b.mn.x);
+        *at(slot, 4) = __float_as_uint(b.mn.y);
+        *at(slot, 5) = __float_as_uint(b.mn.z);
+        *at(slot, 6) = __float_as_uint(b.mx.x);
+        *at(slot, 7) = __float_as_uint(b.mx.y);
+        *at(slot, 8) = __float_as_uint(b.mx.z);
     }
     __device__ uint32_t idx(uint32_t slot) const { return *at(slot, 0); }
     __device__ uint32_t left(uint32_t slot) const { return *at(slot, 1); }
@@ -309,11 +329,13 @@ __global__ void bvh8_batch_init_kernel(uint64_t* pairs, uint32_t slots, MeshBatc
 // batched form (Seg = MeshBatch) the items of all meshes share the queue,
 // the BVH8 index names the mesh, and nodes and leaves are counted per mesh
 // in mesh_nodes / mesh_leaves.
-template <typename Seg, bool AUCTION>
+template <typename Seg, bool AUCTION, bool KIDS>
 __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict__ b2, Seg seg, Node8* out,
                                                         uint32_t cap, uint32_t slots, uint32_t* prim_idx,
                                                         uint64_t* pairs, uint32_t* ctr, uint32_t* mesh_nodes,
-                                                        uint32_t* mesh_leaves, uint32_t* err) {
+                                                        uint32_t* mesh_leaves, uint32_t* err,
+                                                        const ChildPair* __restrict__ kids) {
+    static_assert(!KIDS || !Seg::kBatch, "child-pair records are written by single-mesh builds only");
     extern __shared__ uint32_t s_slots[];
     const SlotTable tab{s_slots};
     const uint32_t lane = lane_id();
@@ -374,6 +396,7 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
         uint32_t base8 = 0, cap8 = cap;
         bool internal = false;
         Node2 nd;
+        ChildPair kp;  // KIDS: the item node's children
         if (ready) {
             if constexpr (Seg::kBatch) {
                 me = seg.span(owner_of(seg.off8, 0, seg.meshes - 1, b8i));
@@ -394,6 +417,20 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
                 }
             } else if (b2i >= node_limit || b8i - base8 >= cap8) {
                 set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
+            } else if constexpr (KIDS) {
+                // an item is an internal node; its box is the union of its children's
+                if (b2i < me.count) {
+                    set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
+                } else {
+                    kp = load_child_pair(kids + (b2i - me.count));
+                    if (kp.li >= node_limit || kp.ri >= node_limit) {
+                        set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
+                    } else {
+                        nd.b = kp.l;
+                        grow(nd.b, kp.r);
+                        internal = true;
+                    }
+                }
             } else {
                 nd = load_node(mb2, b2i);
                 if (nd.left >= node_limit || nd.right >= node_limit)
@@ -407,33 +444,64 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
         uint32_t inner = 0, count = 0, asg = kInvalid, leaf = 0;
         if (internal) {
             // open BVH2 nodes top-down until 8 children or no inner child
-            uint32_t l0 = nd.left, l1 = nd.right;
+            uint32_t l0, l1;
+            if constexpr (KIDS) {
+                l0 = kp.li;
+                l1 = kp.ri;
+            } else {
+                l0 = nd.left;
+                l1 = nd.right;
+            }
             uint32_t msb = 0;
             while (true) {
-                const Node2 c0 = load_node(mb2, l0), c1 = load_node(mb2, l1);
-                if (kPrefetch) {
-                    if (c0.left < node_limit && c0.right < node_limit) {
-                        prefetch_l2(mb2 + c0.left);
-                        prefetch_l2(mb2 + c0.right);
+                bool in0, in1, first;
+                if constexpr (KIDS) {
+                    // the children of the opened node and their boxes are in
+                    // its record; an internal child's own record is the next
+                    // load of its chain
+                    in0 = l0 >= me.count;
+                    in1 = l1 >= me.count;
+                    if (kPrefetch) {
+                        if (in0) prefetch_l2(kids + (l0 - me.count));
+                        if (in1) prefetch_l2(kids + (l1 - me.count));
                     }
-                    if (c1.left < node_limit && c1.right < node_limit) {
-                        prefetch_l2(mb2 + c1.left);
-                        prefetch_l2(mb2 + c1.right);
+                    first = !(half_area(kp.l) < half_area(kp.r));
+                    tab.put(msb, first ? l1 : l0, first ? kp.r : kp.l);
+                    tab.put(count + 1, first ? l0 : l1, first ? kp.l : kp.r);
+                } else {
+                    const Node2 c0 = load_node(mb2, l0), c1 = load_node(mb2, l1);
+                    if (kPrefetch) {
+                        if (c0.left < node_limit && c0.right < node_limit) {
+                            prefetch_l2(mb2 + c0.left);
+                            prefetch_l2(mb2 + c0.right);
+                        }
+                        if (c1.left < node_limit && c1.right < node_limit) {
+                            prefetch_l2(mb2 + c1.left);
+                            prefetch_l2(mb2 + c1.right);
+                        }
                     }
+                    first = !(half_area(c0.b) < half_area(c1.b));
+                    // the smaller-area child takes the re-opened position
+                    tab.put(msb, first ? l1 : l0, first ? c1 : c0);
+                    tab.put(count + 1, first ? l0 : l1, first ? c0 : c1);
+                    in0 = c0.left != kInvalid;
+                    in1 = c1.left != kInvalid;
                 }
-                const bool first = !(half_area(c0.b) < half_area(c1.b));
-                // the smaller-area child takes the re-opened position
-                tab.put(msb, first ? l1 : l0, first ? c1 : c0);
-                tab.put(count + 1, first ? l0 : l1, first ? c0 : c1);
-                if ((first ? c1 : c0).left != kInvalid) inner |= 1u << msb;
-                if ((first ? c0 : c1).left != kInvalid) inner |= 1u << (count + 1);
+                if (first ? in1 : in0) inner |= 1u << msb;
+                if (first ? in0 : in1) inner |= 1u << (count + 1);
                 count += 2;
                 if (inner == 0 || count == 8) break;
                 msb = 31 - __clz(inner);
                 inner &= ~(1u << msb);
                 count--;
-                l0 = tab.left(msb);
-                l1 = tab.right(msb);
+                if constexpr (KIDS) {
+                    kp = load_child_pair(kids + (tab.idx(msb) - me.count));
+                    l0 = kp.li;
+                    l1 = kp.ri;
+                } else {
+                    l0 = tab.left(msb);
+                    l1 = tab.right(msb);
+                }
                 if (l0 >= node_limit || l1 >= node_limit) {  // corrupt BVH2: report, stop expanding
                     set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
                     inner |= 1u << msb;
@@ -504,7 +572,8 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
                         const uint64_t pair = ((uint64_t)tab.idx(a) << 32) | (base8 + child_base + k);
                         st_relaxed_u64(pairs + work_base + k, pair);
                     } else if ((leaf >> i) & 1u) {
-                        prim_idx[me.start + prim_base + popc_below(leaf, i)] = tab.right(a);
+                        // leaf i of the BVH2 is primitive i (its node's right field)
+                        prim_idx[me.start + prim_base + popc_below(leaf, i)] = KIDS ? tab.idx(a) : tab.right(a);
                     }
                 }
                 write_node8(out + b8i, nd.b, tab, child_base, prim_base, asg, inner, leaf);
@@ -519,31 +588,31 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
     }
 }
 
-template <typename Seg, bool AUCTION>
+template <typename Seg, bool AUCTION, bool KIDS>
 cudaError_t configure_smem() {
     return once_per_device([] {
-        return cudaFuncSetAttribute(bvh8_kernel<Seg, AUCTION>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        return cudaFuncSetAttribute(bvh8_kernel<Seg, AUCTION, KIDS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)kSlotSmem);
     });
 }
 
-template <typename Seg, bool AUCTION>
+template <typename Seg, bool AUCTION, bool KIDS>
 uint32_t persistent_grid(uint32_t items) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh8_kernel<Seg, AUCTION>, kThreads, kSlotSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bvh8_kernel<Seg, AUCTION, KIDS>, kThreads, kSlotSmem);
     if (per_sm < 1) per_sm = 1;
     const uint32_t want = (items + kThreads - 1) / kThreads;
     return std::max(1u, std::min(want, (uint32_t)(device_info().sms * per_sm)));
 }
 
-template <typename Seg, bool AUCTION>
+template <typename Seg, bool AUCTION, bool KIDS = false>
 cudaError_t launch_wide(const Node2* bvh2, Seg seg, uint32_t items, Node8* out, uint32_t cap, uint32_t slots,
                         uint32_t* prim_idx, uint64_t* pairs, uint32_t* ctr, uint32_t* mesh_nodes,
-                        uint32_t* mesh_leaves, uint32_t* err, cudaStream_t s) {
-    cudaError_t e = configure_smem<Seg, AUCTION>();
+                        uint32_t* mesh_leaves, uint32_t* err, cudaStream_t s, const ChildPair* kids = nullptr) {
+    cudaError_t e = configure_smem<Seg, AUCTION, KIDS>();
     if (e) return e;
-    bvh8_kernel<Seg, AUCTION><<<persistent_grid<Seg, AUCTION>(items), kThreads, kSlotSmem, s>>>(
-        bvh2, seg, out, cap, slots, prim_idx, pairs, ctr, mesh_nodes, mesh_leaves, err);
+    bvh8_kernel<Seg, AUCTION, KIDS><<<persistent_grid<Seg, AUCTION, KIDS>(items), kThreads, kSlotSmem, s>>>(
+        bvh2, seg, out, cap, slots, prim_idx, pairs, ctr, mesh_nodes, mesh_leaves, err, kids);
     return cudaGetLastError();
 }
 
@@ -555,7 +624,7 @@ cudaError_t run_bvh8_stall_probe(uint32_t* err_out) {
     const uint32_t n = 2;
     unsigned char* buf = nullptr;
     const size_t bytes = 4 * (kBvh8CtrWords + 32) + 3 * sizeof(Node2) + 2 * sizeof(Node8) + 8 * n + 4 * n;
-    cudaError_t e = configure_smem<SingleMesh, false>();
+    cudaError_t e = configure_smem<SingleMesh, false, false>();
     if (!e) e = cudaMalloc(&buf, bytes);
     if (e) return e;
     uint32_t* ctr = (uint32_t*)buf;  // 256-byte aligned
@@ -571,8 +640,8 @@ cudaError_t run_bvh8_stall_probe(uint32_t* err_out) {
     c[kBvh8Pending] = 1;  // ... but its pair is never written
     if (!e) e = cudaMemcpy(ctr, c, sizeof(c), cudaMemcpyHostToDevice);
     if (!e) {
-        bvh8_kernel<SingleMesh, false><<<1, kThreads, kSlotSmem>>>(b2, SingleMesh{n}, out, 2, n, prim, pairs, ctr,
-                                                                   nullptr, nullptr, err);
+        bvh8_kernel<SingleMesh, false, false><<<1, kThreads, kSlotSmem>>>(b2, SingleMesh{n}, out, 2, n, prim, pairs,
+                                                                          ctr, nullptr, nullptr, err, nullptr);
         e = cudaGetLastError();
     }
     if (!e) e = cudaMemcpy(err_out, err, 4, cudaMemcpyDeviceToHost);
@@ -587,12 +656,19 @@ cudaError_t launch_bvh8_init(uint64_t* pairs, uint32_t n, uint32_t* ctr, cudaStr
 }
 
 cudaError_t launch_bvh8(const Node2* bvh2, uint32_t n, Node8* out, uint32_t cap, uint32_t* prim_idx, uint64_t* pairs,
-                        uint32_t* ctr, uint32_t* err, bool auction, cudaStream_t s) {
+                        uint32_t* ctr, uint32_t* err, bool auction, cudaStream_t s, const ChildPair* child_pairs) {
+    const SingleMesh seg{n};
+    if (child_pairs) {
+        if (auction)
+            return launch_wide<SingleMesh, true, true>(bvh2, seg, n, out, cap, n, prim_idx, pairs, ctr, nullptr,
+                                                       nullptr, err, s, child_pairs);
+        return launch_wide<SingleMesh, false, true>(bvh2, seg, n, out, cap, n, prim_idx, pairs, ctr, nullptr,
+                                                    nullptr, err, s, child_pairs);
+    }
     if (auction)
-        return launch_wide<SingleMesh, true>(bvh2, SingleMesh{n}, n, out, cap, n, prim_idx, pairs, ctr, nullptr,
-                                                    nullptr, err, s);
-    return launch_wide<SingleMesh, false>(bvh2, SingleMesh{n}, n, out, cap, n, prim_idx, pairs, ctr, nullptr,
-                                                 nullptr, err, s);
+        return launch_wide<SingleMesh, true>(bvh2, seg, n, out, cap, n, prim_idx, pairs, ctr, nullptr, nullptr, err,
+                                             s);
+    return launch_wide<SingleMesh, false>(bvh2, seg, n, out, cap, n, prim_idx, pairs, ctr, nullptr, nullptr, err, s);
 }
 
 cudaError_t launch_bvh8_batch_init(uint64_t* pairs, uint32_t slots, const MeshBatch& batch, uint32_t* ctr,

@@ -63,9 +63,9 @@ def test_workspace_sizes(lib):
         assert s.bvh2_node_count == 2 * n - 1
         assert s.bvh8_node_capacity == (4 * n - 1 + 6) // 7
         # keys x2, values x2, parent slots, BVH8 work slots, H-PLOC cluster
-        # records, look-back
-        assert s.workspace_bytes >= n * (2 * kb + 8 + 4 + 8 + 32)
-        assert s.workspace_bytes < n * (2 * kb + 8 + 4 + 8 + 32 + 8)
+        # records, child-pair records, look-back
+        assert s.workspace_bytes >= n * (2 * kb + 8 + 4 + 8 + 32 + 64)
+        assert s.workspace_bytes < n * (2 * kb + 8 + 4 + 8 + 32 + 64 + 8)
     assert lib.nxb_query_build_sizes(0, None, ctypes.byref(s)) == 1
     # NXB_BUILD_VALIDATE belongs to the plain calls only
     v = nxb.BuildConfig(validate=True).to_c()
