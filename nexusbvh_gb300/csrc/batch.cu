@@ -39,8 +39,8 @@ uint32_t mesh_bits_of(uint32_t meshes) { return meshes > 1 ? 32u - (uint32_t)__b
 
 // Segment offsets of an arena, in allocation order.
 struct Segments {
-    size_t off, off8, ctrl, scene, zero_end, parent, look, ctr8, mnodes, mleaves, trng, ka, kb, va, vb, pairs, bvh2, bvh8,
-        prim, res, total;
+    size_t off, off8, ctrl, scene, zero_end, parent, look, ctr8, mnodes, mleaves, trng, ka, kb, va, vb, pairs, kids,
+        bvh2, bvh8, prim, res, total;
 };
 
 Segments segments_of(const BatchArena& a) {
@@ -68,6 +68,7 @@ Segments segments_of(const BatchArena& a) {
     g.va = seg(4 * n);
     g.vb = seg(4 * n);
     g.pairs = seg(8ull * a.slots);
+    g.kids = seg(sizeof(ChildPair) * n);
     g.bvh2 = seg(sizeof(Node2) * 2 * n);
     g.bvh8 = seg(sizeof(Node8) * (size_t)a.slots);
     g.prim = seg(4 * n);
@@ -124,6 +125,7 @@ void batch_bind(unsigned char* p, BatchArena* a) {
     a->vals_a = reinterpret_cast<uint32_t*>(p + g.va);
     a->vals_b = reinterpret_cast<uint32_t*>(p + g.vb);
     a->pairs = reinterpret_cast<uint64_t*>(p + g.pairs);
+    a->kids = reinterpret_cast<ChildPair*>(p + g.kids);
     a->bvh2 = reinterpret_cast<Node2*>(p + g.bvh2);
     a->bvh8 = reinterpret_cast<Node8*>(p + g.bvh8);
     a->prim_idx = reinterpret_cast<uint32_t*>(p + g.prim);
@@ -188,7 +190,8 @@ nxb_status batch_enqueue(const BatchArena& a, const void* prims, nxb_prim_type t
         // overlapping H-PLOC of group k+1
         for (uint32_t k = 0; k < g.count; ++k) {
             NXB_TRY(launch_hploc_batch(keys, perm, a.parent, a.bvh2, mb, g.prim[k], g.prim[k + 1], t.radius, tokens,
-                                       a.pol, a.ctrl->leaf_ctr + k, &a.ctrl->error_word, t.hploc_ctas_per_sm, s));
+                                       a.pol, a.ctrl->leaf_ctr + k, &a.ctrl->error_word, t.hploc_ctas_per_sm, s,
+                                       a.kids));
             const uint32_t m0 = g.mesh[k];
             const MeshBatch view{a.off + m0, a.off8 + m0, g.mesh[k + 1] - m0};
             cudaStream_t bs = s;
@@ -199,7 +202,8 @@ nxb_status batch_enqueue(const BatchArena& a, const void* prims, nxb_prim_type t
             }
             NXB_TRY(launch_bvh8_batch(a.bvh2, view, g.prim[k + 1] - g.prim[k], a.bvh8, g.slot[k + 1] - g.slot[k],
                                       a.prim_idx, a.pairs + g.slot[k], a.ctr8 + k * kBvh8CtrWords,
-                                      a.mesh_nodes + m0, a.mesh_leaves + m0, &a.ctrl->error_word, t.auction, bs));
+                                      a.mesh_nodes + m0, a.mesh_leaves + m0, &a.ctrl->error_word, t.auction, bs,
+                                      a.kids));
         }
         if (g.count > 1) {
             NXB_TRY(cudaEventRecord(fork->join, fork->side));

@@ -381,8 +381,8 @@ __device__ __forceinline__ MergeCtx mesh_ctx(const MergeCtx& all, const Seg& seg
         const uint32_t mesh = __shfl_sync(kFullMask, me.m, owner);
         start = __shfl_sync(kFullMask, me.start, owner);
         const uint32_t count = __shfl_sync(kFullMask, me.count, owner);
-        return MergeCtx{all.nodes + 2ull * start, all.tok, all.rec, nullptr, all.parent_of_last + mesh, count,
-                        2 * count - 1, all.err};
+        return MergeCtx{all.nodes + 2ull * start, all.tok, all.rec, all.kids ? all.kids + start : nullptr,
+                        all.parent_of_last + mesh, count, 2 * count - 1, all.err};
     } else {
         start = 0;
         return all;
@@ -559,7 +559,7 @@ __global__ __launch_bounds__(kThreads, hploc_ctas_per_sm<R, Seg>()) void hploc_k
                                                          uint64_t* bvh8_pairs, uint32_t* bvh8_ctr, ChildPair* kids) {
     const uint32_t lane = lane_id();
     if (!Seg::kBatch && bvh8_ctr && blockIdx.x == 0 && threadIdx.x == 0) bvh8_queue_counters(bvh8_ctr);
-    const MergeCtx all{nodes, tok, rec, Seg::kBatch ? nullptr : kids, parent_of_last, end, 2 * end - 1, err};
+    const MergeCtx all{nodes, tok, rec, kids, parent_of_last, end, 2 * end - 1, err};
     // each warp's row for the merge compaction (single-mesh builds)
     __shared__ uint4 s_rows[Seg::kBatch ? 1 : kThreads / 32][64];
     uint4* row = s_rows[Seg::kBatch ? 0 : threadIdx.x >> 5];
@@ -704,9 +704,9 @@ cudaError_t launch_hploc(uint32_t key_bytes, const void* keys, uint32_t* cluster
 cudaError_t launch_hploc_batch(const uint64_t* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
                                const MeshBatch& batch, uint32_t begin, uint32_t end, uint32_t radius,
                                uint32_t* tokens, uint32_t* parent_of_last, uint32_t* leaf_ctr, uint32_t* err,
-                               uint32_t ctas_per_sm, cudaStream_t s) {
+                               uint32_t ctas_per_sm, cudaStream_t s, ChildPair* child_pairs) {
     return launch_t(reinterpret_cast<const MeshKey*>(keys), cluster_idx, parent, nodes, batch, begin, end, radius,
-                    tokens, parent_of_last, leaf_ctr, err, ctas_per_sm, s);
+                    tokens, parent_of_last, leaf_ctr, err, ctas_per_sm, s, nullptr, nullptr, nullptr, child_pairs);
 }
 
 }  // namespace nxb

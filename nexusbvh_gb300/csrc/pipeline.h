@@ -218,11 +218,12 @@ cudaError_t launch_batch_morton(const Node2* nodes, const MeshBatch& batch, uint
 // H-PLOC over the sorted positions [begin, end), which must cover whole
 // meshes; leaf_ctr: a zeroed word of its own.  parent_of_last: one word per
 // mesh holding INVALID on entry; ctas_per_sm caps the persistent grid (0: as
-// many CTAs as fit).
+// many CTAs as fit).  child_pairs (optional): one 64-byte record per
+// primitive of the batch; mesh m's internal node X gets record off[m] + X - n_m.
 cudaError_t launch_hploc_batch(const uint64_t* keys, uint32_t* cluster_idx, uint32_t* parent, Node2* nodes,
                                const MeshBatch& batch, uint32_t begin, uint32_t end, uint32_t radius,
                                uint32_t* tokens, uint32_t* parent_of_last, uint32_t* leaf_ctr, uint32_t* err,
-                               uint32_t ctas_per_sm, cudaStream_t s);
+                               uint32_t ctas_per_sm, cudaStream_t s, ChildPair* child_pairs = nullptr);
 // Meshes cut into consecutive groups whose BVH8 collapses are separate
 // launches: group g holds meshes [mesh[g], mesh[g+1]), primitives
 // [prim[g], prim[g+1]) and BVH8 slots [slot[g], slot[g+1]).
@@ -240,10 +241,12 @@ cudaError_t launch_bvh8_batch_init(uint64_t* pairs, uint32_t slots, const MeshBa
                                    cudaStream_t s);
 // The collapse of the meshes of `batch` (a whole batch, or one group's view:
 // off, off8, mesh_nodes and mesh_leaves advanced to the group's first mesh,
-// pairs to its first slot, ctr to its counters).
+// pairs to its first slot, ctr to its counters).  child_pairs: as for
+// launch_bvh8, the records launch_hploc_batch wrote (mesh m's at off[m]).
 cudaError_t launch_bvh8_batch(const Node2* bvh2, const MeshBatch& batch, uint32_t total, Node8* out, uint32_t slots,
                               uint32_t* prim_idx, uint64_t* pairs, uint32_t* ctr, uint32_t* mesh_nodes,
-                              uint32_t* mesh_leaves, uint32_t* err, bool auction, cudaStream_t s);
+                              uint32_t* mesh_leaves, uint32_t* err, bool auction, cudaStream_t s,
+                              const ChildPair* child_pairs = nullptr);
 cudaError_t launch_batch_finalize(const MeshBatch& batch, const uint32_t* scene_ord, const uint32_t* mesh_nodes,
                                   const uint32_t* mesh_leaves, nxb_batch_mesh* out, cudaStream_t s);
 // One batched build's device memory (a single allocation carved into
@@ -280,6 +283,7 @@ struct BatchArena {
     uint32_t* vals_a = nullptr;
     uint32_t* vals_b = nullptr;
     uint64_t* pairs = nullptr;
+    ChildPair* kids = nullptr;  // child-pair records (one per primitive, 64-byte aligned)
     Node2* bvh2 = nullptr;
     Node8* bvh8 = nullptr;
     uint32_t* prim_idx = nullptr;

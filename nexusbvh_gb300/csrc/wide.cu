@@ -335,7 +335,6 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
                                                         uint64_t* pairs, uint32_t* ctr, uint32_t* mesh_nodes,
                                                         uint32_t* mesh_leaves, uint32_t* err,
                                                         const ChildPair* __restrict__ kids) {
-    static_assert(!KIDS || !Seg::kBatch, "child-pair records are written by single-mesh builds only");
     extern __shared__ uint32_t s_slots[];
     const SlotTable tab{s_slots};
     const uint32_t lane = lane_id();
@@ -422,7 +421,7 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
                 if (b2i < me.count) {
                     set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
                 } else {
-                    kp = load_child_pair(kids + (b2i - me.count));
+                    kp = load_child_pair(kids + me.start + (b2i - me.count));
                     if (kp.li >= node_limit || kp.ri >= node_limit) {
                         set_error(err, NXB_DEVERR_BVH8_OVERFLOW);
                     } else {
@@ -462,8 +461,8 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
                     in0 = l0 >= me.count;
                     in1 = l1 >= me.count;
                     if (kPrefetch) {
-                        if (in0) prefetch_l2(kids + (l0 - me.count));
-                        if (in1) prefetch_l2(kids + (l1 - me.count));
+                        if (in0) prefetch_l2(kids + me.start + (l0 - me.count));
+                        if (in1) prefetch_l2(kids + me.start + (l1 - me.count));
                     }
                     first = !(half_area(kp.l) < half_area(kp.r));
                     tab.put(msb, first ? l1 : l0, first ? kp.r : kp.l);
@@ -495,7 +494,7 @@ __global__ __launch_bounds__(kThreads) void bvh8_kernel(const Node2* __restrict_
                 inner &= ~(1u << msb);
                 count--;
                 if constexpr (KIDS) {
-                    kp = load_child_pair(kids + (tab.idx(msb) - me.count));
+                    kp = load_child_pair(kids + me.start + (tab.idx(msb) - me.count));
                     l0 = kp.li;
                     l1 = kp.ri;
                 } else {
@@ -681,7 +680,15 @@ cudaError_t launch_bvh8_batch_init(uint64_t* pairs, uint32_t slots, const MeshBa
 
 cudaError_t launch_bvh8_batch(const Node2* bvh2, const MeshBatch& batch, uint32_t total, Node8* out, uint32_t slots,
                               uint32_t* prim_idx, uint64_t* pairs, uint32_t* ctr, uint32_t* mesh_nodes,
-                              uint32_t* mesh_leaves, uint32_t* err, bool auction, cudaStream_t s) {
+                              uint32_t* mesh_leaves, uint32_t* err, bool auction, cudaStream_t s,
+                              const ChildPair* child_pairs) {
+    if (child_pairs) {
+        if (auction)
+            return launch_wide<MeshBatch, true, true>(bvh2, batch, total, out, 0u, slots, prim_idx, pairs, ctr,
+                                                      mesh_nodes, mesh_leaves, err, s, child_pairs);
+        return launch_wide<MeshBatch, false, true>(bvh2, batch, total, out, 0u, slots, prim_idx, pairs, ctr,
+                                                   mesh_nodes, mesh_leaves, err, s, child_pairs);
+    }
     if (auction)
         return launch_wide<MeshBatch, true>(bvh2, batch, total, out, 0u, slots, prim_idx, pairs, ctr, mesh_nodes,
                                             mesh_leaves, err, s);
