@@ -730,6 +730,7 @@ def measure_served(args, world, rank, local, requests: int, warmup: int, burst: 
         device or copied from pinned host memory before each build."""
         out = nxb.CBVH8()
         lat = []
+        copies = []  # (bytes, start event, end event) of the large host-input copies
         d_in = torch.empty((max(n for _, n, _ in reqs), 9), dtype=torch.float32, device="cuda")
         t0 = time.perf_counter()
         arr = t0 + arrivals_of(gaps)
@@ -742,7 +743,14 @@ def measure_served(args, world, rank, local, requests: int, warmup: int, burst: 
             c = nxb.BuildConfig(prioritize_speed=kb == 30).to_c()
             src = dev[kind]
             if not on_device:
+                ev = None
+                if i >= warm and n >= 1_000_000:
+                    ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                    ev[0].record()
                 d_in[:n].copy_(host[kind][:n], non_blocking=True)
+                if ev:
+                    ev[1].record()
+                    copies.append((36 * n, ev[0], ev[1]))
                 src = d_in
             nxb.check(lib.nxb_build_bvh8(src.data_ptr(), nxb.NXB_PRIM_TRIANGLE, n, ctypes.byref(c),
                                          stream_ptr, ctypes.byref(out), None), "nxb_build_bvh8")
@@ -751,9 +759,17 @@ def measure_served(args, world, rank, local, requests: int, warmup: int, burst: 
                 lat.append((time.perf_counter() - arr[i]) * 1e3)
         wall = time.perf_counter() - (start_timed or t0)
         tris = sum(n for _, n, _ in reqs[warm:])
-        return {"p50_ms": _pctl(lat, 50), "p99_ms": _pctl(lat, 99), "mean_ms": float(np.mean(lat)),
-                "max_ms": float(np.max(lat)), "wall_s": wall, "builds_s": len(lat) / wall,
-                "mtris_s": tris / wall / 1e6}
+        r = {"p50_ms": _pctl(lat, 50), "p99_ms": _pctl(lat, 99), "mean_ms": float(np.mean(lat)),
+             "max_ms": float(np.max(lat)), "wall_s": wall, "builds_s": len(lat) / wall,
+             "mtris_s": tris / wall / 1e6}
+        if copies:
+            # the host link as this pass saw it: GB/s of each large input copy
+            torch.cuda.synchronize()
+            gbs = [b / (e0.elapsed_time(e1) * 1e-3) / 1e9 for b, e0, e1 in copies]
+            r["h2d_gbs_min"] = float(np.min(gbs))
+            r["h2d_gbs_median"] = float(np.median(gbs))
+            r["h2d_copies"] = len(gbs)
+        return r
 
     total = warmup + requests
     reqs = served_requests(total)
