@@ -27,7 +27,7 @@ FULL = [("clustered12m", 63, 8), ("clustered12m", 63, 16), ("sphere4m", 30, 8), 
 def test_full_size_chain(gpu, orc, name, key_bits, radius):
     prims = scenes.by_name(name)
     n = prims.shape[0]
-    chain = run_chain(prims, key_bits, orc, radius=radius)
+    chain = run_chain(prims, key_bits, orc, radius=radius, whole=False)
     out = S.build_async(prims, key_bits, radius=radius)
     b8 = S.host(out.nodes.reshape(-1)).view(nxb.BVH8_NODE_DTYPE)
     prim = S.host(out.prim_idx).view(np.uint32)

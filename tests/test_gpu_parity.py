@@ -62,7 +62,11 @@ CASES = [
 ]
 
 
-def run_chain(prims, key_bits, orc, radius=8):
+def run_chain(prims, key_bits, orc, radius=8, whole=True):
+    """The stage chain against the oracle fed each previous GPU stage; with
+    `whole`, also the whole pipeline (nxb_build_async, whose collapse reads
+    the child-pair records H-PLOC writes instead of the BVH2 nodes) against
+    that chain."""
     n = prims.shape[0]
     d_nodes, d_scene = S.stage_bounds(prims)
     leaves_g = S.nodes2(d_nodes)[:n]
@@ -113,6 +117,14 @@ def run_chain(prims, key_bits, orc, radius=8):
     c8g, c8o = S.cost_bvh8(b8_g, rb), orc.bvh8_cost(b8_g, rb)
     assert abs(c2g - c2o) <= 1e-3 * abs(c2o)
     assert abs(c8g - c8o) <= 1e-3 * abs(c8o)
+    if whole:
+        out = S.build_async(prims, key_bits, radius=radius)
+        w2 = S.nodes2(out.bvh2.nodes.view(-1))
+        assert orc.compare_bvh2(w2, 2 * n - 2, b2_g, 2 * n - 2, n) == 0, "whole-pipeline BVH2 differs"
+        w8 = S.host(out.nodes.reshape(-1)).view(nxb.BVH8_NODE_DTYPE)
+        wp = S.host(out.prim_idx).view(np.uint32)
+        assert out.node_count == nc
+        assert orc.compare_bvh8(w8, wp, b8_g, prim_g, n) == 0, "whole-pipeline BVH8 differs"
     return dict(b2=b2_g, b8=b8_g, prim=prim_g, leaves=leaves_g, morton_diffs=morton_diffs, rep8=rep8,
                 costs=(c2g, c8g))
 
