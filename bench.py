@@ -373,6 +373,9 @@ def run_ours(args, world, rank, local):
             "traffic": traffic,
             "peak_source": pk["source"],
             "issue_frac": per_stage[dominant].get("issue_frac"),
+            **({"traffic_note": "includes the 64 B/tri child-pair records H-PLOC writes for the BVH8 "
+                                "collapse, which then reads them instead of the BVH2 nodes"}
+               if dominant == "hploc" and traffic else {}),
         },
         "e2e": {"value": round(e2e_value, 2), "unit": "Mtris/s", "h2d_bytes_per_step": 36 * n,
                 "d2h_bytes_per_step": ctypes.sizeof(nxb.CResult),
