@@ -197,7 +197,9 @@ nxb_status nxb_read_bvh8(const char* path, nxb_bvh8* host_bvh);
 /* Sizes, in bytes, of what a build of prim_count primitives needs.  All
  * device buffers must be 256-byte aligned (cudaMalloc alignment). */
 typedef struct nxb_build_sizes {
-    size_t workspace_bytes;  /* scratch: keys, values, sort state, counters */
+    size_t workspace_bytes;  /* scratch: keys, values, sort state, counters, H-PLOC cluster records and
+                              * the child-pair records a BVH8 build reads (64 bytes per primitive; a
+                              * build without a BVH8 may pass a workspace that much smaller) */
     size_t bvh2_node_count;  /* 2n-1 */
     size_t bvh8_node_capacity; /* ceil((4n-1)/7), the reference's worst case */
 } nxb_build_sizes;

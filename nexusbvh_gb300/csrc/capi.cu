@@ -57,6 +57,7 @@ struct Layout {
     size_t tiles_words = 0;  // look-back words for all passes
     size_t ctrl = 0, result = 0, cost = 0, keys_a = 0, keys_b = 0, vals_a = 0, vals_b = 0, lookback = 0, parent = 0,
            pairs = 0, records = 0, kids = 0, total = 0;
+    size_t total_bvh2 = 0;  // a build that stops at the BVH2 needs no child-pair records (the last segment)
 };
 
 Layout make_layout(uint32_t n, uint32_t key_bits) {
@@ -87,6 +88,7 @@ Layout make_layout(uint32_t n, uint32_t key_bits) {
     L.parent = seg(4ull * n);
     L.pairs = seg(8ull * n);
     L.records = seg(32ull * n);
+    L.total_bvh2 = off;
     L.kids = seg(64ull * n);
     L.total = off;
     return L;
@@ -153,7 +155,7 @@ nxb_status enqueue_build(const void* prims, nxb_prim_type type, uint32_t n, cons
                          nxb_build_result* result, cudaStream_t s, StageEvents* evs) {
     const uint32_t key_bits = key_bits_of(cfg);
     const Layout L = make_layout(n, key_bits);
-    if (ws_bytes < L.total) return NXB_ERR_WORKSPACE_TOO_SMALL;
+    if (ws_bytes < (bvh8 ? L.total : L.total_bvh2)) return NXB_ERR_WORKSPACE_TOO_SMALL;
     Control* ctrl = reinterpret_cast<Control*>(ws + L.ctrl);
     void* keys_a = ws + L.keys_a;
     void* keys_b = ws + L.keys_b;
@@ -249,7 +251,8 @@ nxb_status build_plain(const void* prims, nxb_prim_type type, uint32_t n, const 
     bool have_events = false;
     nxb_status status = NXB_OK;
     nxb_build_result res{};
-    cudaError_t e = cudaMallocAsync((void**)&ws, L.total, s);
+    const size_t ws_bytes = wide ? L.total : L.total_bvh2;
+    cudaError_t e = cudaMallocAsync((void**)&ws, ws_bytes, s);
     if (!e) e = cudaMallocAsync((void**)&bvh2, sizeof(Node2) * (2ull * n - 1), s);
     if (!e && wide) e = cudaMallocAsync((void**)&bvh8, sizeof(Node8) * bvh8_capacity(n), s);
     if (!e && wide) e = cudaMallocAsync((void**)&prim_idx, 4ull * n, s);
@@ -262,7 +265,7 @@ nxb_status build_plain(const void* prims, nxb_prim_type type, uint32_t n, const 
     } else {
         nxb_build_result* d_res = reinterpret_cast<nxb_build_result*>(ws + L.result);
         float* d_cost = reinterpret_cast<float*>(ws + L.cost);
-        status = enqueue_build(prims, type, n, cfg, ws, L.total, bvh2, bvh8, prim_idx, d_res, s,
+        status = enqueue_build(prims, type, n, cfg, ws, ws_bytes, bvh2, bvh8, prim_idx, d_res, s,
                                have_events ? &evs : nullptr);
         if (status == NXB_OK && metrics) {
             e = launch_bvh2_cost(bvh2, 2 * n - 1, &d_res->scene_bounds, d_cost, s);

@@ -256,9 +256,18 @@ def test_errors_are_status_codes(gpu):
     s = b.sizes(1000, cfg)
     ws = torch.empty(s.workspace_bytes - 256, dtype=torch.uint8, device="cuda")
     nodes = torch.empty((s.bvh2_node_count, 32), dtype=torch.uint8, device="cuda")
+    b8 = torch.empty((s.bvh8_node_capacity, 80), dtype=torch.uint8, device="cuda")
+    prim_idx = torch.empty(1000, dtype=torch.int32, device="cuda")
     res = torch.zeros(64, dtype=torch.uint8, device="cuda")
     with pytest.raises(nxb.NxbError) as ei:
-        b.enqueue(prims, 1000, cfg, ws, nodes, None, None, res)
+        b.enqueue(prims, 1000, cfg, ws, nodes, b8, prim_idx, res)
+    assert ei.value.status == 5
+    # a build that stops at the BVH2 needs no child-pair records (64 bytes per primitive)
+    small = torch.empty(s.workspace_bytes - 64 * 1000, dtype=torch.uint8, device="cuda")
+    b.enqueue(prims, 1000, cfg, small, nodes, None, None, res)
+    torch.cuda.synchronize()
+    with pytest.raises(nxb.NxbError) as ei:
+        b.enqueue(prims, 1000, cfg, small[:-256], nodes, None, None, res)
     assert ei.value.status == 5
     bad = nxb.BuildConfig(search_radius=7)
     with pytest.raises(nxb.NxbError) as ei:
