@@ -54,6 +54,21 @@ def test_argument_checks_need_no_device(lib):
     assert lib.nxb_build_bvh8(16, 1, 10, ctypes.byref(c), None, None, None) == 1
 
 
+def test_workspace_requirement_needs_no_device(lib):
+    """nxb_build_async rejects a short workspace before it touches the
+    device: a BVH8 build needs the queried size, a build that stops at the
+    BVH2 needs 64 bytes per primitive less (no child-pair records)."""
+    n = 100_000
+    c = nxb.BuildConfig().to_c()
+    s = nxb.CSizes()
+    assert lib.nxb_query_build_sizes(n, ctypes.byref(c), ctypes.byref(s)) == 0
+    fake = 1 << 20  # 256-byte aligned addresses the call never dereferences before this check
+    short_bvh8 = s.workspace_bytes - 1
+    assert lib.nxb_build_async(fake, 1, n, ctypes.byref(c), fake, short_bvh8, fake, fake, fake, fake, None) == 5
+    short_bvh2 = s.workspace_bytes - 64 * n - 1
+    assert lib.nxb_build_async(fake, 1, n, ctypes.byref(c), fake, short_bvh2, fake, None, None, fake, None) == 5
+
+
 def test_workspace_sizes(lib):
     s = nxb.CSizes()
     for bits, kb in ((30, 4), (63, 8)):
