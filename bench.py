@@ -255,14 +255,20 @@ def run_ours(args, world, rank, local):
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
+    copy_evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                for _ in range(e2e_steps)]
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    for k in range(e2e_steps):
+        copy_evs[k][0].record()
         d_in.copy_(h_prims, non_blocking=True)
+        copy_evs[k][1].record()
         nxb.check(lib.nxb_build_bvh8(d_in.data_ptr(), nxb.NXB_PRIM_TRIANGLE, n, ctypes.byref(c), sptr,
                                      ctypes.byref(out), None), "nxb_build_bvh8")
         nxb.check(lib.nxb_free_device_bvh8(ctypes.byref(out)), "nxb_free_device_bvh8")
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
+    # the host link as the e2e steps saw it (their input copies, timed on the stream)
+    copy_ms = statistics.median(e0.elapsed_time(e1) for e0, e1 in copy_evs)
     if world > 1:
         t = torch.tensor([e2e_s], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -379,7 +385,8 @@ def run_ours(args, world, rank, local):
         },
         "e2e": {"value": round(e2e_value, 2), "unit": "Mtris/s", "h2d_bytes_per_step": 36 * n,
                 "d2h_bytes_per_step": ctypes.sizeof(nxb.CResult),
-                "call": "nxb_build_bvh8 (C ABI, allocates outputs) after a pinned host->device copy"},
+                "call": "nxb_build_bvh8 (C ABI, allocates outputs) after a pinned host->device copy",
+                "copy_ms": round(copy_ms, 3), "h2d_gbs": round(36 * n / (copy_ms * 1e-3) / 1e9, 1)},
         # per build: bounds, Morton, the sort (30-bit: 4 passes; 63-bit: 4
         # passes, the bucket sort and the fallback launch), H-PLOC (which
         # also initialises the BVH8 work queue), BVH8, finalize
